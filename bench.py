@@ -1,0 +1,350 @@
+#!/usr/bin/env python3
+"""Benchmark: shooter steps per second of the progressive-refinement loop.
+
+Workload: the 64x64-quad room with 16 seeded boxes (61,440 triangles,
+-converge at 1e-4 of an emitter's key, -adapt_area 5 -delta_ff 5e-6
+-triangle 200000), FP32 solver.  A step is one shooter step: select the
+shooter and shoot it to every receiver (the reference's parallelRadiosity).
+
+Our arm (default): the scene is resident in HBM; W warm-up steps, then K
+timed steps, each timed on the device with CUDA events on the solver's own
+stream; L2 is flushed (a 512 MB write) before every timed step because the
+scene is smaller than L2.  Also reported:
+  roofline      the shooting kernel's algorithmic bytes per launch (176 B per
+                slot streamed + 8 B per walk cell, 24 B per triangle test,
+                48 B per edge test, counts taken exactly from a counting pass
+                over the same steps) over its event-timed duration, against
+                the measured HBM copy bandwidth;
+  e2e           the same steps through the C ABI from host buffers: device
+                upload of the scene, K steps, download of the results;
+  cpu_baseline  the reference's own CPU solver (built from its sources, when
+                available; else the C restatement) on the machine's host cores.
+--impl reference times the reference's CPU solver alone on the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(REPO, "hw-radiosity_gb300"))
+
+WORKLOAD = "room64x64_boxes16 (61,440 triangles, config 2), FP32, plain single-scene form"
+BYTES_PER_SLOT = 176       # selection key 16 + receiver read 112 + receiver write 48
+BYTES_PER_CELL = 8
+BYTES_PER_TRI_TEST = 24
+BYTES_PER_SE_TEST = 48
+
+
+def _peaks():
+    p = os.path.join(REPO, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled while the GPU works."""
+
+    def __init__(self, index: int):
+        self.index = index
+        self.samples = []
+        self.proc = None
+        self.thread = None
+
+    def start(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+            return
+
+        def reader():
+            for line in self.proc.stdout:
+                f = [x.strip() for x in line.split(",")]
+                if len(f) >= 9:
+                    self.samples.append(f)
+
+        self.thread = threading.Thread(target=reader, daemon=True)
+        self.thread.start()
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=5)
+
+    def summary(self):
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+        sm = [num(s[1]) for s in self.samples if num(s[1]) is not None]
+        mx = [num(s[2]) for s in self.samples if num(s[2]) is not None]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for s in self.samples:
+            for k, name in enumerate(names):
+                if s[5 + k].lower().startswith("active"):
+                    reasons.add(name)
+        loaded = [x for x in sm if mx and x >= 0.5 * max(mx)] or sm
+        return {"sm_mhz": statistics.median(loaded) if loaded else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.samples)}
+
+
+def _nproc():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def _scene_file(tmp):
+    from hwrad import scenes
+    sc = scenes.config2()
+    return sc, sc.write(os.path.join(tmp, "config2.tri"))
+
+
+def cpu_reference(tri, argv, warmup, steps, prefer_ref=True):
+    """Time the reference's CPU solver (or the C restatement) over steps
+    [warmup, warmup+steps) from its per-step timestamps."""
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import runner
+    cores = _nproc()
+    if prefer_ref and not os.path.exists(runner.REF32):
+        try:
+            runner.build_ref()
+        except Exception:
+            pass
+    if prefer_ref and os.path.exists(runner.REF32):
+        binary, kind, jobs = runner.REF32, "reference", cores
+    else:
+        runner.build_oracle()
+        binary, kind, jobs = runner.ORACLE32, "port", 1
+    wd = tempfile.mkdtemp(prefix="radcpu_")
+    times = os.path.join(wd, "times.txt")
+    t0 = time.time()
+    runner.run(binary, tri, list(argv) + ["-jobs", str(jobs)], steps=warmup + steps,
+               env={"RAD_TIMES": times}, workdir=wd, timeout=3600)
+    wall = time.time() - t0
+    stamps = [float(x) for x in open(times).read().split()]
+    # stamp k = start of step k (0-based); the last stamp is the call that stopped the loop
+    a, b = stamps[warmup], stamps[min(warmup + steps, len(stamps) - 1)]
+    n = min(warmup + steps, len(stamps) - 1) - warmup
+    return {"value": n / (b - a) if b > a else None, "unit": "shots/s", "cores": jobs, "kind": kind,
+            "sample": f"steps {warmup}..{warmup + n} of the workload ({n} shooter steps after {warmup} "
+                      f"warm-up steps; {wall:.1f} s wall including the solver's own init)",
+            "seconds": b - a}
+
+
+def run_reference_arm(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    with tempfile.TemporaryDirectory() as tmp:
+        sc, tri = _scene_file(tmp)
+        res = cpu_reference(tri, sc.argv(), args.warmup, args.steps)
+    line = {"metric": "shots/s", "value": res["value"], "unit": "shots/s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1000.0 / res["value"] if res["value"] else None,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded generator, hwrad.scenes.config2)", "impl": "reference",
+            "config": {"workload": WORKLOAD, "l2": "n/a (CPU)"},
+            "cpu_baseline": {"value": res["value"], "unit": "shots/s", "cores": res["cores"], "kind": res["kind"],
+                             "sample": res["sample"]},
+            "e2e": {"value": res["value"], "unit": "shots/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=500)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference_arm(args)
+
+    import numpy as np
+    import torch
+    from hwrad import capi
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    def barrier():
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    def max_over_ranks(x):
+        if not dist:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    tmp = tempfile.mkdtemp(prefix="radbench_")
+    sc_gen, tri = _scene_file(tmp)
+    argv = sc_gen.argv()
+    opts = capi.options_from_argv(argv, jobs=_nproc())
+    t0 = time.time()
+    scene = capi.Scene.load(tri, opts)
+    tree = capi.Octree(scene, _nproc())
+    scene.init()
+    scene.prepartition()
+    host_prep_s = time.time() - t0
+    n_slots = scene.view()["n"]
+
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def flush_l2():
+        flush.add_(1.0)
+        torch.cuda.synchronize()
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    # ---- timed region: W warm-up steps, K timed steps, L2 flushed before each
+    dev = capi.Device(scene, tree, opts, local)
+    dev.run(args.warmup)
+    barrier()
+    total_ms = 0.0
+    done = 0
+    for _ in range(args.steps):
+        flush_l2()
+        n, conv, ms = dev.run_timed(1)
+        total_ms += ms
+        done += n
+        if conv:
+            break
+    barrier()
+    worst_ms = max_over_ranks(total_ms)
+    # steady state without the flush (graph chunks of 32 steps)
+    n_ss, _, ms_ss = dev.run_timed(args.steps)
+    st_main = dev.stats()
+    dev.close()
+
+    # ---- per-kernel durations over the same steps (fresh instance, one launch at a time)
+    dprof = capi.Device(scene, tree, opts, local)
+    dprof.run(args.warmup)
+    setup_ms = shoot_ms = 0.0
+    for _ in range(done):
+        flush_l2()
+        _, _, a, b = dprof.run_profiled(1)
+        setup_ms += a
+        shoot_ms += b
+    dprof.close()
+
+    # ---- exact walk counts over the same steps (deterministic solver)
+    dcnt = capi.Device(scene, tree, opts, local)
+    dcnt.set_counting(True)
+    dcnt.run(args.warmup)
+    c0 = dcnt.stats()
+    dcnt.run(done)
+    c1 = dcnt.stats()
+    dcnt.close()
+
+    # ---- e2e: C ABI with host buffers (upload, K steps, download)
+    barrier()
+    te0 = time.perf_counter()
+    dev2 = capi.Device(scene, tree, opts, local)
+    n_e2e, _, _ = dev2.run(args.warmup + done)
+    dev2.download(scene)
+    torch.cuda.synchronize()
+    te1 = time.perf_counter()
+    e2e_s = max_over_ranks(te1 - te0)
+    dev_bytes = dev2.stats()["device_bytes"]
+    dev2.close()
+    clocks.stop()
+
+    d = {k: c1[k] - c0[k] for k in ("rays", "rays_ref", "cells", "tri_tests", "se_tests", "prec_steps")}
+    alg_bytes = n_slots * BYTES_PER_SLOT * done + d["cells"] * BYTES_PER_CELL + \
+        d["tri_tests"] * BYTES_PER_TRI_TEST + d["se_tests"] * BYTES_PER_SE_TEST
+    per_launch = alg_bytes / max(done, 1)
+    avg_shoot_s = shoot_ms / 1000.0 / max(done, 1)
+    peak, peak_kind = _peaks()
+    achieved = per_launch / avg_shoot_s / 1e9 if avg_shoot_s > 0 else None
+    traffic = None
+    tp = os.path.join(REPO, "profiles", "k_shoot_traffic.json")
+    if os.path.exists(tp):
+        with open(tp) as fh:
+            traffic = json.load(fh).get("dram_bytes_per_launch")
+
+    value = world * done / (worst_ms / 1000.0) if worst_ms > 0 else None
+    h2d = 0
+    # the upload: slot records (6 x 16 B per slot, 3 of them x3) + octree; approximated by device bytes held
+    h2d = dev_bytes / max(args.warmup + done, 1)
+    d2h = n_slots * 16 * 4 / max(args.warmup + done, 1)
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        try:
+            cpu = cpu_reference(tri, argv, 2, 60)
+        except Exception as exc:
+            cpu = {"value": None, "unit": "shots/s", "cores": _nproc(), "kind": "reference",
+                   "sample": f"failed: {exc}"}
+        cpu = {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")}
+
+    line = {
+        "metric": "shots/s", "value": value, "unit": "shots/s", "n_gpus": world, "steps": done,
+        "warmup": args.warmup, "ms_per_step": worst_ms / max(done, 1), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded generator, hwrad.scenes.config2)",
+        "config": {"workload": WORKLOAD, "slots": n_slots, "l2": "flushed (512 MB write) before every timed step",
+                   "parallelism": f"replicas x{world}", "host_prep_s": round(host_prep_s, 3)},
+        "rays_per_s": d["rays"] / (worst_ms / 1000.0) if worst_ms > 0 else None,
+        "rays_per_step": d["rays"] / max(done, 1),
+        "steady_state": {"value": n_ss / (ms_ss / 1000.0) if ms_ss > 0 else None, "unit": "shots/s",
+                         "note": "graph chunks of 32 steps, no L2 flush", "steps": n_ss},
+        "kernels_ms_per_step": {"k_setup": setup_ms / max(done, 1), "k_shoot": shoot_ms / max(done, 1)},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak if achieved else None, "traffic": traffic,
+                     "kernel": "k_shoot", "peak_kind": f"{peak_kind} hbm_gbs (burst)",
+                     "alg_bytes_per_launch": per_launch,
+                     "counts_per_launch": {k: v / max(done, 1) for k, v in d.items()}},
+        "e2e": {"value": world * (args.warmup + done) / e2e_s, "unit": "shots/s",
+                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "note": "rad_dev_create (upload) + run + rad_dev_download over warm-up + timed steps"},
+        "gpu_launches": 2 * done,
+        "clocks": clocks.summary(),
+        "cpu_baseline": cpu,
+    }
+    if rank == 0:
+        print(json.dumps(line))
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

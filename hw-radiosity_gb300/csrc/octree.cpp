@@ -1,0 +1,234 @@
+// Visibility structure: the reference's uniform-subdivision octree
+// (src/raycast.cpp:168-233), built on the host and flattened for the device.
+//
+// What the walk needs from the tree is (1) the leaf containing a point and
+// (2) each leaf's box and triangle list.  TreeNodeNum (raycast.cpp:254-281)
+// finds the leaf by descending on the bits of the integer cell coordinate
+// gnum = (int)((q - G0) / MinGridLen), so the leaf is a function of the three
+// cell coordinates alone; we tabulate it once for every coordinate triple
+// (at most ~65^3 entries for MaxLevel 6) and the device does one lookup
+// instead of up to six dependent node reads.
+//
+// Subtrees below the root are built concurrently; leaves are renumbered
+// afterwards.  Leaf numbering is free (the walk only compares the leaves of
+// consecutive steps), and each list keeps the reference's order (ascending
+// triangle id, as every list is a filtered copy of 0..n-1).
+#include <algorithm>
+#include <atomic>
+#include <cstring>
+#include <future>
+#include <thread>
+
+#include "rad_host.h"
+
+namespace radgb {
+namespace {
+
+template <typename T>
+struct Box { T g0[3], g1[3]; };
+
+// segment p0-p1 against the rectangle [g0,g1] in dims (x, y), raycast.cpp:24-60
+template <typename T>
+bool segment_meets_rect(const T* p0, const T* p1, const T* g0, const T* g1, int x, int y) {
+    const unsigned o0 = (p0[x] < g0[x]) | (p0[x] > g1[x]) << 1 | (p0[y] < g0[y]) << 2 | (p0[y] > g1[y]) << 3;
+    const unsigned o1 = (p1[x] < g0[x]) | (p1[x] > g1[x]) << 1 | (p1[y] < g0[y]) << 2 | (p1[y] > g1[y]) << 3;
+    if (o0 & o1) return false;
+    if (!(o0 | o1)) return true;
+    const T a = p1[y] - p0[y], b = p1[x] - p0[x];
+    const T c00 = a * (g0[x] - p0[x]) - b * (g0[y] - p0[y]);
+    if (c00 == 0) return true;
+    const bool neg = c00 < 0;
+    // the line misses the rectangle iff all four corners lie strictly on one side
+    if ((a * (g0[x] - p0[x]) - b * (g1[y] - p0[y]) < 0) != neg) return true;
+    if ((a * (g1[x] - p0[x]) - b * (g0[y] - p0[y]) < 0) != neg) return true;
+    if ((a * (g1[x] - p0[x]) - b * (g1[y] - p0[y]) < 0) != neg) return true;
+    return false;
+}
+
+// point on segment hi-lo where coordinate d equals g, raycast.cpp:91-100
+template <typename T>
+void at_coord(const T* hi, const T* lo, T g, int d, T* out) {
+    const T dd = hi[d] - lo[d];
+    if (dd == 0.0) { out[0] = hi[0]; out[1] = hi[1]; out[2] = hi[2]; return; }
+    const T wa = (g - lo[d]) / dd, wb = (hi[d] - g) / dd;
+    for (int k = 0; k < 3; k++) out[k] = wa * hi[k] + wb * lo[k];
+}
+
+// does the triangle meet the cube [g0,g1]; raycast.cpp:109-155
+template <typename T>
+bool tri_meets_box(const T (*p)[3], const T* g0, const T* g1) {
+    const T *hi = p[0], *mid = p[1], *lo = p[2];
+    T a[3], b[3];
+    for (int x = 0; x < 3; x++) {
+        // order the three vertex pointers by coordinate x (raycast.cpp:66-85)
+        if (hi[x] < mid[x]) std::swap(hi, mid);
+        if (hi[x] < lo[x]) std::swap(hi, lo);
+        if (mid[x] < lo[x]) std::swap(mid, lo);
+        const int y = (x + 1) % 3, z = (x + 2) % 3;
+        if (g1[x] < lo[x]) return false;
+        at_coord(hi, lo, g1[x], x, a);
+        if (g1[x] < mid[x]) { at_coord(mid, lo, g1[x], x, b); return segment_meets_rect(a, b, g0, g1, y, z); }
+        if (g1[x] <= hi[x]) { at_coord(hi, mid, g1[x], x, b); return segment_meets_rect(a, b, g0, g1, y, z); }
+        if (g0[x] > hi[x]) return false;
+        at_coord(hi, lo, g0[x], x, a);
+        if (g0[x] > mid[x]) { at_coord(hi, mid, g0[x], x, b); return segment_meets_rect(a, b, g0, g1, y, z); }
+        if (g0[x] >= lo[x]) { at_coord(mid, lo, g0[x], x, b); return segment_meets_rect(a, b, g0, g1, y, z); }
+    }
+    return true;
+}
+
+struct Node { int32_t child[8]; int32_t leaf; };
+
+template <typename T>
+struct Part {                      // one independently built subtree
+    std::vector<Node> nodes;
+    std::vector<Box<T>> leaf_box;
+    std::vector<int32_t> leaf_begin;    // into entries (local)
+    std::vector<int32_t> entries;
+    int64_t n_list = 0;
+    T min_edge;
+};
+
+template <typename T>
+struct Builder {
+    const Scene<T>& s;
+
+    void child_box(const Box<T>& b, int i, Box<T>& c) const {
+        T mid[3];
+        for (int k = 0; k < 3; k++) mid[k] = (T)(0.5 * (double)b.g0[k] + 0.5 * (double)b.g1[k]);
+        for (int j = 0; j < 3; j++) {
+            c.g0[j] = b.g0[j];
+            c.g1[j] = b.g1[j];
+            if ((i >> j) & 1) c.g0[j] = mid[j]; else c.g1[j] = mid[j];
+        }
+    }
+    void filter(const std::vector<int32_t>& in, const Box<T>& c, std::vector<int32_t>& out) const {
+        out.clear();
+        for (int32_t t : in)
+            if (tri_meets_box<T>(s.slots[t].p, c.g0, c.g1)) out.push_back(t);
+    }
+    bool is_leaf(size_t n, int level) const { return n <= (size_t)kMaxTriPerNode || level >= kMaxLevel; }
+
+    int32_t build(Part<T>& P, const std::vector<int32_t>& idx, int level, const Box<T>& b) const {
+        const int32_t id = (int32_t)P.nodes.size();
+        P.nodes.push_back(Node());
+        if (is_leaf(idx.size(), level)) {
+            Node& nd = P.nodes[id];
+            for (int i = 0; i < 8; i++) nd.child[i] = -1;
+            nd.leaf = (int32_t)P.leaf_box.size();
+            P.leaf_box.push_back(b);
+            P.leaf_begin.push_back((int32_t)P.entries.size());
+            P.entries.insert(P.entries.end(), idx.begin(), idx.end());
+            P.n_list += (int64_t)idx.size() + 1;
+            const T edge0 = b.g1[0] - b.g0[0];
+            if (edge0 < P.min_edge) P.min_edge = edge0;
+            return id;
+        }
+        P.nodes[id].leaf = -1;
+        std::vector<int32_t> sub;
+        for (int i = 0; i < 8; i++) {
+            Box<T> c;
+            child_box(b, i, c);
+            filter(idx, c, sub);
+            const int32_t ch = build(P, sub, level + 1, c);
+            P.nodes[id].child[i] = ch;
+        }
+        return id;
+    }
+};
+
+// append part Q (a subtree) into P; returns Q's root id in P
+template <typename T>
+int32_t merge(Part<T>& P, const Part<T>& Q) {
+    const int32_t noff = (int32_t)P.nodes.size(), loff = (int32_t)P.leaf_box.size();
+    const int32_t eoff = (int32_t)P.entries.size();
+    for (Node nd : Q.nodes) {
+        for (int i = 0; i < 8; i++) if (nd.child[i] >= 0) nd.child[i] += noff;
+        if (nd.leaf >= 0) nd.leaf += loff;
+        P.nodes.push_back(nd);
+    }
+    P.leaf_box.insert(P.leaf_box.end(), Q.leaf_box.begin(), Q.leaf_box.end());
+    for (int32_t b : Q.leaf_begin) P.leaf_begin.push_back(b + eoff);
+    P.entries.insert(P.entries.end(), Q.entries.begin(), Q.entries.end());
+    P.n_list += Q.n_list;
+    if (Q.min_edge < P.min_edge) P.min_edge = Q.min_edge;
+    return noff;
+}
+
+}  // namespace
+
+template <typename T>
+void build_octree(const Scene<T>& s, Octree<T>& o, int threads) {
+    Builder<T> B{s};
+    Box<T> root;
+    for (int k = 0; k < 3; k++) { root.g0[k] = s.G0[k]; root.g1[k] = s.G1[k]; o.G0[k] = s.G0[k]; o.G1[k] = s.G1[k]; }
+    std::vector<int32_t> all((size_t)s.n_orig);
+    for (int32_t i = 0; i < s.n_orig; i++) all[i] = i;
+
+    Part<T> P;
+    P.min_edge = s.G1[0] - s.G0[0];                       // raycast.cpp:226
+    if (B.is_leaf(all.size(), 0) || threads <= 1) {
+        B.build(P, all, 0, root);
+    } else {
+        // root built here; its 8 subtrees (level 1) built concurrently
+        P.nodes.push_back(Node());
+        P.nodes[0].leaf = -1;
+        std::vector<Part<T>> parts(8);
+        std::vector<std::future<void>> fut;
+        std::vector<Box<T>> cb(8);
+        for (int i = 0; i < 8; i++) B.child_box(root, i, cb[i]);
+        int nthreads = std::max(1, std::min(threads, 8));
+        std::vector<std::thread> pool;
+        std::atomic<int> next{0};
+        for (int t = 0; t < nthreads; t++)
+            pool.emplace_back([&]() {
+                std::vector<int32_t> sub;
+                for (int i; (i = next.fetch_add(1)) < 8;) {
+                    parts[i].min_edge = P.min_edge;
+                    B.filter(all, cb[i], sub);
+                    B.build(parts[i], sub, 1, cb[i]);
+                }
+            });
+        for (auto& th : pool) th.join();
+        for (int i = 0; i < 8; i++) P.nodes[0].child[i] = merge(P, parts[i]);
+    }
+
+    const int32_t n_leaves = (int32_t)P.leaf_box.size();
+    o.min_grid = P.min_edge;
+    o.grid_num = (int32_t)((s.G1[0] - s.G0[0]) / o.min_grid);   // raycast.cpp:230
+    o.ref_nodes = (int64_t)P.nodes.size();
+    o.ref_list = P.n_list;
+    o.leaf_box.assign((size_t)n_leaves * 8, (T)0);
+    o.leaf_range.assign((size_t)n_leaves * 2, 0);
+    for (int32_t l = 0; l < n_leaves; l++) {
+        for (int k = 0; k < 3; k++) { o.leaf_box[l * 8 + k] = P.leaf_box[l].g0[k]; o.leaf_box[l * 8 + 4 + k] = P.leaf_box[l].g1[k]; }
+        o.leaf_range[l * 2] = P.leaf_begin[l];
+        o.leaf_range[l * 2 + 1] = (l + 1 < n_leaves) ? P.leaf_begin[l + 1] : (int32_t)P.entries.size();
+    }
+    o.entry_tri = std::move(P.entries);
+
+    // cell table: leaf of every cell-coordinate triple (TreeNodeNum's descent)
+    for (int a = 0; a < 3; a++) o.dims[a] = cell_coord<T>(s.G1[a], s.G0[a], o.min_grid) + 1;
+    const size_t ncell = (size_t)o.dims[0] * o.dims[1] * o.dims[2];
+    o.cell_leaf.assign(ncell, -1);
+    for (int gx = 0; gx < o.dims[0]; gx++)
+        for (int gy = 0; gy < o.dims[1]; gy++)
+            for (int gz = 0; gz < o.dims[2]; gz++) {
+                int g[3] = {gx, gy, gz};
+                int32_t cur = 0;
+                int gs = o.grid_num;
+                while (P.nodes[cur].leaf < 0) {
+                    gs >>= 1;
+                    int ix = 0;
+                    for (int i = 0; i < 3; i++)
+                        if (g[i] >= gs) { ix |= 1 << i; g[i] -= gs; }
+                    cur = P.nodes[cur].child[ix];
+                }
+                o.cell_leaf[((size_t)gx * o.dims[1] + gy) * o.dims[2] + gz] = P.nodes[cur].leaf;
+            }
+}
+
+template void build_octree<float>(const Scene<float>&, Octree<float>&, int);
+template void build_octree<double>(const Scene<double>&, Octree<double>&, int);
+
+}  // namespace radgb

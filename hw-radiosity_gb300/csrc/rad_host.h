@@ -1,0 +1,91 @@
+// Host-side scene store and visibility-structure builder (internal C++ API).
+//
+// The host owns topology work that is sequential by definition (scene input,
+// the greedy pre-partition, neighbour links, output); the device owns the
+// shooting loop.  Everything is templated on the solver's scalar type T:
+// float reproduces the reference's FP32 build, double its float->double build.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "rad_gb300.h"
+
+namespace radgb {
+
+constexpr double kPi = 3.1415926535897932;   // include/rad.h:5
+constexpr int kMaxLevel = 6;                 // include/rad.h:7
+constexpr int kMaxTriPerNode = 10;           // include/rad.h:12
+constexpr int kMaxTriPool = 1000000;         // include/rad.h:9 (slot pool hard cap)
+
+// One triangle slot with every field the reference's Triangle carries
+// (include/rad.h:25-39).  Slots past the live count keep whatever the last
+// occupant left, exactly like the reference's static pool, because the
+// pre-partition copies whole slots and reads fields it never initialises.
+template <typename T>
+struct Slot {
+    T p[3][3];
+    int32_t Frgb[3];
+    int32_t Brgb[3];
+    T accB[3][3];
+    T daccB[3][3];
+    T deltaB[3];
+    T se[3][4];
+    T c[3];
+    T n[3];
+    T area;
+    int32_t parent;
+    int32_t nb[3];
+};
+
+template <typename T>
+struct Scene {
+    std::vector<Slot<T>> slots;   // pool, zero-filled; [0, trinum) live
+    int32_t trinum = 0;           // live slots
+    int32_t n_orig = 0;           // triangles read from the input (the octree indexes these)
+    T G0[3] = {0, 0, 0};
+    T G1[3] = {0, 0, 0};
+    T minarea = 0, maxarea = 0;
+    rad_options opt{};
+    bool alloc_warned = false;
+    std::string log;              // info lines the CLI prints
+};
+
+// Flattened visibility structure.  Leaves are numbered in the order they
+// are created; only their identity matters to the walk (it compares the leaf
+// of consecutive steps), and every leaf list keeps the reference's order.
+template <typename T>
+struct Octree {
+    T G0[3], G1[3];
+    T min_grid = 0;               // smallest leaf edge (raycast.cpp:184-185)
+    int32_t grid_num = 0;         // raycast.cpp:230
+    int32_t dims[3] = {0, 0, 0};  // cell-table extent per axis (max cell coordinate + 1)
+    std::vector<int32_t> cell_leaf;     // dims[0]*dims[1]*dims[2] -> leaf id
+    std::vector<T> leaf_box;            // 8 per leaf: g0.xyz, 0, g1.xyz, 0
+    std::vector<int32_t> leaf_range;    // 2 per leaf: [begin, end) into entry_tri
+    std::vector<int32_t> entry_tri;     // triangle id per list entry
+    int64_t ref_nodes = 0;        // node and list-slot counts the reference reports
+    int64_t ref_list = 0;
+};
+
+// Scene input / output, src/rad.cpp:47-111 and 117-242.
+template <typename T> int load_tri_text(const char* text, size_t len, const rad_options& o, Scene<T>& s, std::string& err);
+template <typename T> int load_arrays(const float* vtx, const int32_t* frgb, const int32_t* brgb, int32_t n,
+                                      const rad_options& o, Scene<T>& s, std::string& err);
+template <typename T> void init_radiosity(Scene<T>& s);              // src/rad.cpp:259-356
+template <typename T> void prepartition(Scene<T>& s);                // src/shade.cpp:556-598
+template <typename T> int write_fin(const Scene<T>& s, const char* prefix, int loop, std::string& err);
+template <typename T> void build_octree(const Scene<T>& s, Octree<T>& o, int threads);  // raycast.cpp:216-233
+
+// Cell coordinate along one axis, raycast.cpp:263 (shared with the device).
+template <typename T>
+inline int cell_coord(T q, T g0, T min_grid) {
+    return (int)(((double)q - (double)g0) / (double)min_grid);
+}
+
+// Float to text with the semantics of include/float2string.h's
+// fp::tostring<float>: returns false (and writes nothing) where it would.
+bool format_float(float x, char* buf);
+
+}  // namespace radgb

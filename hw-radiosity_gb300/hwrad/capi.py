@@ -1,0 +1,327 @@
+"""ctypes binding of the C ABI in ``include/rad_gb300.h``.
+
+The Python side is a thin mirror of the reference's flow (``src/rad.cpp``
+``main`` -> ``InitModelFromFile`` -> ``DoRadiosity``): load a ``.tri`` scene,
+build the visibility structure, initialise, pre-partition, run the shooting
+loop on the device, read the results back.  The library must have been built
+(``hwrad.build.build()``); there is no fallback path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from typing import Dict, Optional, Sequence
+
+import numpy as np
+
+from . import build as _build
+
+RAD_OK = 0
+RAD_ERR_ARG, RAD_ERR_IO, RAD_ERR_PARSE, RAD_ERR_CAPACITY, RAD_ERR_CUDA, RAD_ERR_WALK, RAD_ERR_NODEV = range(1, 8)
+
+EXPORTS = [
+    "rad_options_default", "rad_last_error", "rad_version",
+    "rad_scene_load", "rad_scene_from_arrays", "rad_scene_init", "rad_scene_prepartition",
+    "rad_scene_view_get", "rad_scene_write_fin", "rad_scene_log", "rad_scene_free",
+    "rad_octree_build", "rad_octree_info", "rad_octree_free",
+    "rad_dev_create", "rad_dev_run", "rad_dev_run_timed", "rad_dev_run_profiled", "rad_dev_download", "rad_dev_trace", "rad_dev_stats",
+    "rad_dev_set_counting", "rad_dev_ray_hit", "rad_dev_form_factors", "rad_dev_destroy",
+]
+
+
+class Options(C.Structure):
+    _fields_ = [("debug", C.c_int32), ("adapt_area", C.c_float), ("sample_area", C.c_float),
+                ("converge", C.c_float), ("delta_ff", C.c_float), ("write_cycle", C.c_int32),
+                ("zip", C.c_int32), ("triangle_limit", C.c_int32), ("light_scale", C.c_float),
+                ("interactive", C.c_int32), ("jobs", C.c_int32), ("parallel_src", C.c_int32),
+                ("precision", C.c_int32), ("walk_cap", C.c_int32)]
+
+
+class SceneView(C.Structure):
+    _fields_ = [("n", C.c_int32), ("n_orig", C.c_int32), ("elem_size", C.c_int32),
+                ("p", C.c_void_p), ("accB", C.c_void_p), ("deltaB", C.c_void_p), ("area", C.c_void_p),
+                ("nrm", C.c_void_p), ("ctr", C.c_void_p), ("parent", C.c_void_p), ("frgb", C.c_void_p),
+                ("brgb", C.c_void_p), ("nb", C.c_void_p), ("G0", C.c_float * 3), ("G1", C.c_float * 3),
+                ("sample_area", C.c_float), ("min_area", C.c_float), ("max_area", C.c_float)]
+
+
+class Stats(C.Structure):
+    _fields_ = [("steps", C.c_int64), ("shots", C.c_int64), ("rays", C.c_int64), ("rays_ref", C.c_int64),
+                ("cells", C.c_int64), ("tri_tests", C.c_int64), ("se_tests", C.c_int64),
+                ("prec_steps", C.c_int64), ("walk_cap_hits", C.c_int64), ("converged", C.c_int32),
+                ("n_slots", C.c_int32), ("device_bytes", C.c_int64)]
+
+
+class RadError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"[{code}] {msg}")
+        self.code = code
+
+
+_lib: Optional[C.CDLL] = None
+
+
+def lib_path() -> str:
+    return _build.LIB
+
+
+def load(path: Optional[str] = None) -> C.CDLL:
+    """Load the native library (it must exist: there is no fallback)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    p = path or _build.LIB
+    if not os.path.exists(p):
+        raise RuntimeError(f"native library {p} missing; run hwrad.build.build() first")
+    L = C.CDLL(p)
+    vp, i32, i64, f = C.c_void_p, C.c_int32, C.c_int64, C.c_float
+    P = C.POINTER
+    sig = {
+        "rad_options_default": (None, [P(Options)]),
+        "rad_last_error": (C.c_char_p, []),
+        "rad_version": (C.c_char_p, []),
+        "rad_scene_load": (C.c_int, [C.c_char_p, P(Options), P(vp)]),
+        "rad_scene_from_arrays": (C.c_int, [vp, vp, vp, i32, P(Options), P(vp)]),
+        "rad_scene_init": (C.c_int, [vp]),
+        "rad_scene_prepartition": (C.c_int, [vp]),
+        "rad_scene_view_get": (C.c_int, [vp, P(SceneView)]),
+        "rad_scene_write_fin": (C.c_int, [vp, C.c_char_p, i32]),
+        "rad_scene_log": (C.c_char_p, [vp, i32]),
+        "rad_scene_free": (None, [vp]),
+        "rad_octree_build": (C.c_int, [vp, i32, P(vp)]),
+        "rad_octree_info": (C.c_int, [vp, P(i64), P(i64), P(i32), P(i64), P(i32)]),
+        "rad_octree_free": (None, [vp]),
+        "rad_dev_create": (C.c_int, [vp, vp, P(Options), i32, P(vp)]),
+        "rad_dev_run": (C.c_int, [vp, i64, P(i64), P(i32)]),
+        "rad_dev_run_timed": (C.c_int, [vp, i64, P(i64), P(i32), P(C.c_double)]),
+        "rad_dev_run_profiled": (C.c_int, [vp, i64, P(i64), P(i32), P(C.c_double), P(C.c_double)]),
+        "rad_dev_download": (C.c_int, [vp, vp]),
+        "rad_dev_trace": (C.c_int, [vp, vp, i64, P(i64)]),
+        "rad_dev_stats": (C.c_int, [vp, P(Stats)]),
+        "rad_dev_set_counting": (C.c_int, [vp, i32]),
+        "rad_dev_ray_hit": (C.c_int, [vp, vp, vp, vp, i32, vp]),
+        "rad_dev_form_factors": (C.c_int, [vp, i32, vp, i32, vp]),
+        "rad_dev_destroy": (None, [vp]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = L
+    return L
+
+
+def _check(rc: int, allow=()):
+    if rc != RAD_OK and rc not in allow:
+        raise RadError(rc, load().rad_last_error().decode(errors="replace"))
+    return rc
+
+
+def options(**kw) -> Options:
+    o = Options()
+    load().rad_options_default(C.byref(o))
+    for k, v in kw.items():
+        setattr(o, k, v)
+    return o
+
+
+def options_from_argv(args: Sequence[str], **kw) -> Options:
+    """Reference CLI options (e.g. ["-converge", "4.5", "-light", "0.0588"])."""
+    m = {"-debug": ("debug", int), "-adapt_area": ("adapt_area", float), "-sample_area": ("sample_area", float),
+         "-converge": ("converge", float), "-delta_ff": ("delta_ff", float), "-write_cycle": ("write_cycle", int),
+         "-triangle": ("triangle_limit", int), "-light": ("light_scale", float), "-jobs": ("jobs", int),
+         "-parallel_src": ("parallel_src", int)}
+    o = options(**kw)
+    a = list(args)
+    i = 0
+    while i < len(a):
+        if a[i] in m:
+            name, ty = m[a[i]]
+            setattr(o, name, ty(a[i + 1]))
+            i += 2
+        elif a[i] == "-zip":
+            o.zip = 1
+            i += 1
+        elif a[i] == "-interactive":
+            o.interactive = 1
+            i += 1
+        else:
+            i += 1
+    return o
+
+
+class Scene:
+    """Host scene store (``rad_scene``)."""
+
+    def __init__(self, handle, opts: Options):
+        self.h = C.c_void_p(handle)
+        self.opts = opts
+
+    @classmethod
+    def load(cls, path: str, opts: Options) -> "Scene":
+        h = C.c_void_p()
+        _check(load().rad_scene_load(path.encode(), C.byref(opts), C.byref(h)))
+        return cls(h.value, opts)
+
+    @classmethod
+    def from_arrays(cls, vtx: np.ndarray, frgb: np.ndarray, brgb: np.ndarray, opts: Options) -> "Scene":
+        vtx = np.ascontiguousarray(vtx, np.float32).reshape(-1, 9)
+        frgb = np.ascontiguousarray(frgb, np.int32).reshape(-1, 3)
+        brgb = np.ascontiguousarray(brgb, np.int32).reshape(-1, 3)
+        h = C.c_void_p()
+        _check(load().rad_scene_from_arrays(vtx.ctypes.data, frgb.ctypes.data, brgb.ctypes.data, len(vtx),
+                                            C.byref(opts), C.byref(h)))
+        return cls(h.value, opts)
+
+    def init(self):
+        _check(load().rad_scene_init(self.h))
+
+    def prepartition(self):
+        _check(load().rad_scene_prepartition(self.h))
+
+    def log(self, stream: int = 2) -> str:
+        return load().rad_scene_log(self.h, stream).decode(errors="replace")
+
+    def view(self) -> Dict[str, np.ndarray]:
+        v = SceneView()
+        _check(load().rad_scene_view_get(self.h, C.byref(v)))
+        n = v.n
+        ft = np.float32 if v.elem_size == 4 else np.float64
+
+        def arr(ptr, dt, cols):
+            if n == 0:
+                return np.zeros((0, cols) if cols > 1 else (0,), dt)
+            a = np.ctypeslib.as_array(C.cast(ptr, C.POINTER(np.ctypeslib.as_ctypes_type(dt))), (n * cols,)).copy()
+            return a.reshape(n, cols) if cols > 1 else a
+
+        return {"n": n, "n_orig": v.n_orig, "p": arr(v.p, ft, 9), "accB": arr(v.accB, ft, 9),
+                "deltaB": arr(v.deltaB, ft, 3), "area": arr(v.area, ft, 1), "n_": arr(v.nrm, ft, 3),
+                "c": arr(v.ctr, ft, 3), "parent": arr(v.parent, np.int32, 1), "Frgb": arr(v.frgb, np.int32, 3),
+                "Brgb": arr(v.brgb, np.int32, 3), "nb": arr(v.nb, np.int32, 3),
+                "G0": np.array(v.G0[:], np.float32), "G1": np.array(v.G1[:], np.float32),
+                "sample_area": v.sample_area}
+
+    def write_fin(self, prefix: str, loop: int = 0):
+        _check(load().rad_scene_write_fin(self.h, prefix.encode(), loop))
+
+    def close(self):
+        if self.h:
+            load().rad_scene_free(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Octree:
+    def __init__(self, scene: Scene, threads: int = 0):
+        self.h = C.c_void_p()
+        _check(load().rad_octree_build(scene.h, threads, C.byref(self.h)))
+
+    def info(self) -> Dict[str, object]:
+        a, b, e = C.c_int64(), C.c_int64(), C.c_int64()
+        nl = C.c_int32()
+        dims = (C.c_int32 * 3)()
+        _check(load().rad_octree_info(self.h, C.byref(a), C.byref(b), C.byref(nl), C.byref(e), dims))
+        return {"ref_nodes": a.value, "ref_list": b.value, "leaves": nl.value, "entries": e.value,
+                "dims": list(dims)}
+
+    def close(self):
+        if self.h:
+            load().rad_octree_free(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Device:
+    """Device-resident solver (``rad_dev``)."""
+
+    def __init__(self, scene: Scene, tree: Octree, opts: Options, device: int = 0):
+        self.h = C.c_void_p()
+        self.P = max(1, opts.parallel_src)
+        _check(load().rad_dev_create(scene.h, tree.h, C.byref(opts), device, C.byref(self.h)))
+
+    def run(self, max_steps: int = 1 << 62):
+        sd = C.c_int64()
+        cv = C.c_int32()
+        rc = _check(load().rad_dev_run(self.h, max_steps, C.byref(sd), C.byref(cv)), allow=(RAD_ERR_WALK,))
+        return sd.value, bool(cv.value), rc
+
+    def run_timed(self, max_steps: int):
+        """(steps, converged, device milliseconds) for up to max_steps steps."""
+        sd, cv, ms = C.c_int64(), C.c_int32(), C.c_double()
+        _check(load().rad_dev_run_timed(self.h, max_steps, C.byref(sd), C.byref(cv), C.byref(ms)),
+               allow=(RAD_ERR_WALK,))
+        return sd.value, bool(cv.value), ms.value
+
+    def run_profiled(self, max_steps: int):
+        """(steps, converged, setup-kernel ms, shoot-kernel ms), one launch at a time."""
+        sd, cv, a, b = C.c_int64(), C.c_int32(), C.c_double(), C.c_double()
+        _check(load().rad_dev_run_profiled(self.h, max_steps, C.byref(sd), C.byref(cv), C.byref(a), C.byref(b)),
+               allow=(RAD_ERR_WALK,))
+        return sd.value, bool(cv.value), a.value, b.value
+
+    def download(self, scene: Scene):
+        _check(load().rad_dev_download(self.h, scene.h))
+
+    def trace(self) -> np.ndarray:
+        n = C.c_int64()
+        _check(load().rad_dev_trace(self.h, None, 0, C.byref(n)))
+        out = np.zeros(n.value, np.int32)
+        if n.value:
+            _check(load().rad_dev_trace(self.h, out.ctypes.data, n.value, C.byref(n)))
+        return out.reshape(-1, self.P)
+
+    def stats(self) -> Dict[str, int]:
+        s = Stats()
+        _check(load().rad_dev_stats(self.h, C.byref(s)))
+        return {k: getattr(s, k) for k, _ in Stats._fields_}
+
+    def set_counting(self, on: bool):
+        _check(load().rad_dev_set_counting(self.h, 1 if on else 0))
+
+    def ray_hit(self, p: np.ndarray, v: np.ndarray, ban: np.ndarray, dtype=np.float32) -> np.ndarray:
+        p = np.ascontiguousarray(p, dtype).reshape(-1, 3)
+        v = np.ascontiguousarray(v, dtype).reshape(-1, 3)
+        ban = np.ascontiguousarray(ban, np.int32).reshape(-1)
+        out = np.zeros(len(p), np.int32)
+        _check(load().rad_dev_ray_hit(self.h, p.ctypes.data, v.ctypes.data, ban.ctypes.data, len(p),
+                                      out.ctypes.data))
+        return out
+
+    def form_factors(self, src: int, rcv: np.ndarray, dtype=np.float32) -> np.ndarray:
+        rcv = np.ascontiguousarray(rcv, np.int32).reshape(-1)
+        out = np.zeros((len(rcv), 3), dtype)
+        _check(load().rad_dev_form_factors(self.h, int(src), rcv.ctypes.data, len(rcv), out.ctypes.data))
+        return out
+
+    def close(self):
+        if self.h:
+            load().rad_dev_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def solve(tri_path: str, opts: Options, device: int = 0, max_steps: int = 1 << 62):
+    """The reference's flow end to end: returns (scene, device solver, steps, converged)."""
+    sc = Scene.load(tri_path, opts)
+    tree = Octree(sc, opts.jobs)
+    sc.init()
+    sc.prepartition()
+    dv = Device(sc, tree, opts, device)
+    steps, conv, _ = dv.run(max_steps)
+    dv.download(sc)
+    return sc, dv, steps, conv

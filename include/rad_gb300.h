@@ -1,0 +1,175 @@
+/*
+ * rad_gb300.h -- C ABI of the GB300 progressive-refinement radiosity solver.
+ *
+ * Drop-in replacement for the shooting loop of morris821028/hw-radiosity.
+ * The reference keeps its state in globals (TriStore[], trinum, G0, G1:
+ * include/rad.h:51-55, src/rad.cpp:33-36) and calls, per shooter step,
+ * listCanditate() -> Shade() -> AdaptCalFF()/CalFF() -> RayHitted()
+ * (src/rad.cpp:387-451, src/shade.cpp:107-168, 435-462, src/raycast.cpp:335-360).
+ * Here the host keeps the topology work (scene input, neighbour links,
+ * pre-partition, output) and the device keeps the mesh, the visibility
+ * structure and the unshot energy resident in HBM and runs the whole loop.
+ *
+ * Conventions: every call returns RAD_OK (0) or an RAD_ERR_* code and leaves a
+ * one-line message for rad_last_error() (thread-local).  Handles are not
+ * re-entrant: drive one handle from one host thread; separate handles are
+ * independent.  Plain pointers and sizes only.
+ */
+#ifndef RAD_GB300_H
+#define RAD_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define RAD_OK 0
+#define RAD_ERR_ARG 1        /* bad argument */
+#define RAD_ERR_IO 2         /* file could not be opened or written */
+#define RAD_ERR_PARSE 3      /* malformed .tri input (reference: assert in ReadVector/ReadIVector) */
+#define RAD_ERR_CAPACITY 4   /* a size exceeds a stated limit */
+#define RAD_ERR_CUDA 5       /* a CUDA runtime call failed */
+#define RAD_ERR_WALK 6       /* a visibility walk hit its step cap (result for that ray: not visible) */
+#define RAD_ERR_NODEV 7      /* no CUDA device */
+
+/* Solver options: the reference's command-line globals (src/rad.cpp:17-31),
+ * same names, meaning and defaults, plus two extensions at the end. */
+typedef struct rad_options {
+    int32_t debug;          /* -debug        Debug = 0 */
+    float adapt_area;       /* -adapt_area   AreaLimit = 5.0 */
+    float sample_area;      /* -sample_area  SampleArea = -1 (model dependent: max area / 100) */
+    float converge;         /* -converge     ConvergeLimit = 1200.0 (absolute unshot key) */
+    float delta_ff;         /* -delta_ff     DeltaFFLimit = 5e-6 */
+    int32_t write_cycle;    /* -write_cycle  WriteIteration = 10 */
+    int32_t zip;            /* -zip          CompressResult = 0 */
+    int32_t triangle_limit; /* -triangle     TriangleLimit = 1000000 */
+    float light_scale;      /* -light        LightScale = 1.0 */
+    int32_t interactive;    /* -interactive  InteractiveOutput = 0 */
+    int32_t jobs;           /* -jobs         host threads for host-side steps (default 2) */
+    int32_t parallel_src;   /* -parallel_src ParallelSource = 1 (shooters per step) */
+    /* extensions */
+    int32_t precision;      /* 32: FP32 solver (reference FP32 build); 64: all-FP64 form */
+    int32_t walk_cap;       /* max cell steps per visibility walk (default 1<<20) */
+} rad_options;
+
+typedef struct rad_scene rad_scene;   /* host scene store */
+typedef struct rad_octree rad_octree; /* host-built visibility structure */
+typedef struct rad_dev rad_dev;       /* device-resident solver */
+
+/* Read-only view of a scene's live slots (valid until the scene changes or
+ * is freed).  Arrays are slot-major; element type float (precision 32) or
+ * double (precision 64) for the real-valued fields. */
+typedef struct rad_scene_view {
+    int32_t n;              /* live slots (trinum) */
+    int32_t n_orig;         /* triangles read from the input */
+    int32_t elem_size;      /* 4 or 8 */
+    const void* p;          /* n*9  vertices p[3][3] */
+    const void* accB;       /* n*9  accumulated radiosity per vertex and channel */
+    const void* deltaB;     /* n*3  unshot radiosity per channel */
+    const void* area;       /* n */
+    const void* nrm;        /* n*3  unit normal */
+    const void* ctr;        /* n*3  centre */
+    const int32_t* parent;  /* n    original triangle id, -1 for a split (logical) slot */
+    const int32_t* frgb;    /* n*3  reflectance 0..255 */
+    const int32_t* brgb;    /* n*3  emission; a channel == 255 marks a light */
+    const int32_t* nb;      /* n*3  neighbour across edge p0-p1, p1-p2, p2-p0 */
+    float G0[3], G1[3];     /* grid corners (as float) */
+    float sample_area;      /* resolved SampleArea */
+    float min_area, max_area;
+} rad_scene_view;
+
+/* Statistics of a device run. */
+typedef struct rad_stats {
+    int64_t steps;          /* shooter steps executed (calls of parallelRadiosity that shot) */
+    int64_t shots;          /* shooters processed (steps * shooters per step) */
+    int64_t rays;           /* visibility walks issued */
+    int64_t rays_ref;       /* walks the reference issues for the same work (adds the
+                               whole-source walk AdaptCalFF discards, src/shade.cpp:141-168) */
+    int64_t cells;          /* octree cells visited (0 unless counting is on) */
+    int64_t tri_tests;      /* ray/triangle plane tests (0 unless counting is on) */
+    int64_t se_tests;       /* edge-plane tests after a plane hit (0 unless counting is on) */
+    int64_t prec_steps;     /* "Precision Exceeded" re-steps, src/raycast.cpp:344-351 */
+    int64_t walk_cap_hits;  /* walks stopped by walk_cap */
+    int32_t converged;      /* 1 once a selection found no candidate */
+    int32_t n_slots;
+    int64_t device_bytes;   /* device memory held by the handle */
+} rad_stats;
+
+void rad_options_default(rad_options* o);
+const char* rad_last_error(void);
+const char* rad_version(void);
+
+/* ---- host scene store --------------------------------------------------- */
+
+/* ReadTriangle, src/rad.cpp:47-111 (+ the "Read #Triangle" line of
+ * InitModelFromFile, src/rad.cpp:244-252). */
+int rad_scene_load(const char* path, const rad_options* o, rad_scene** out);
+/* Same from arrays: vtx[n*9] (float), frgb[n*3], brgb[n*3]. */
+int rad_scene_from_arrays(const float* vtx, const int32_t* frgb, const int32_t* brgb, int32_t n,
+                          const rad_options* o, rad_scene** out);
+/* InitRadiosity, src/rad.cpp:259-356: light energy, neighbour links
+ * (exact-coordinate edge matching through a hash instead of the O(N^2) scan,
+ * same final links as the sequential scan), SampleArea. */
+int rad_scene_init(rad_scene* s);
+/* PrePartitionTriangles, src/shade.cpp:556-598 (greedy longest-edge
+ * bisection of the largest non-light triangles until area < 1 or the pool
+ * is full). */
+int rad_scene_prepartition(rad_scene* s);
+int rad_scene_view_get(const rad_scene* s, rad_scene_view* v);
+/* PrintOut, src/rad.cpp:117-242: prefix.fin (loop 0) or prefix.<loop>. */
+int rad_scene_write_fin(const rad_scene* s, const char* prefix, int32_t loop);
+/* Info lines (reference wording) produced by the last host-side call. */
+const char* rad_scene_log(const rad_scene* s, int32_t stream); /* 1 = stdout lines, 2 = stderr lines */
+void rad_scene_free(rad_scene* s);
+
+/* ---- visibility structure ---------------------------------------------- */
+
+/* BuildTree, src/raycast.cpp:168-233, over the scene's original triangles
+ * (call before rad_scene_prepartition, as the reference does).  Reports the
+ * reference's #TreeNode / #Trilist counts. */
+int rad_octree_build(const rad_scene* s, int32_t threads, rad_octree** out);
+int rad_octree_info(const rad_octree* t, int64_t* ref_nodes, int64_t* ref_list, int32_t* n_leaves,
+                    int64_t* n_entries, int32_t dims[3]);
+void rad_octree_free(rad_octree* t);
+
+/* ---- device solver ------------------------------------------------------ */
+
+/* Upload the scene (after init + pre-partition) and the visibility structure
+ * to device `device`.  The walk's triangle records are taken from the
+ * scene's current slots, as RayHitted reads TriStore at shooting time. */
+int rad_dev_create(const rad_scene* s, const rad_octree* t, const rad_options* o, int32_t device, rad_dev** out);
+/* Run up to max_steps shooter steps (parallelRadiosity, src/rad.cpp:406-451,
+ * each: select -> shoot to every receiver -> zero the shooters).  Stops early
+ * when a selection finds no candidate (*converged = 1).  Steps are issued in
+ * CUDA-graph chunks; the host synchronises once per chunk. */
+int rad_dev_run(rad_dev* d, int64_t max_steps, int64_t* steps_done, int32_t* converged);
+/* rad_dev_run, also reporting the device time of the executed steps in
+ * milliseconds (CUDA events on the solver's stream around the graph
+ * launches; host synchronisation is outside the measured interval). */
+int rad_dev_run_timed(rad_dev* d, int64_t max_steps, int64_t* steps_done, int32_t* converged, double* device_ms);
+/* Steps one kernel launch at a time (no graph) with CUDA events around each
+ * kernel: *ms_setup and *ms_shoot receive the summed durations of the
+ * selection/setup kernel and the shooting kernel. */
+int rad_dev_run_profiled(rad_dev* d, int64_t max_steps, int64_t* steps_done, int32_t* converged, double* ms_setup,
+                         double* ms_shoot);
+/* Copy accB and deltaB back into the scene's slots. */
+int rad_dev_download(rad_dev* d, rad_scene* s);
+/* Shooter ids chosen so far, in order (P per step; -1 pads a short step). */
+int rad_dev_trace(const rad_dev* d, int32_t* out, int64_t cap, int64_t* n);
+int rad_dev_stats(const rad_dev* d, rad_stats* st);
+/* Count cells / triangle tests / edge tests during later steps (slower). */
+int rad_dev_set_counting(rad_dev* d, int32_t on);
+/* Batched RayHitted (src/raycast.cpp:335-360): for each i, the triangle the
+ * walk from p[i] along v[i] (not normalised) stops at, skipping ban[i]; -1 if
+ * it leaves the grid.  Host arrays in and out (precision 32: float). */
+int rad_dev_ray_hit(rad_dev* d, const void* p, const void* v, const int32_t* ban, int32_t n, int32_t* hit);
+/* Batched Shade form factors without deposit: ff[i*3+v] for receiver slot
+ * rcv[i] from shooter slot src (AdaptCalFF(CalFF(...)), src/shade.cpp:442-450). */
+int rad_dev_form_factors(rad_dev* d, int32_t src, const int32_t* rcv, int32_t n, void* ff);
+void rad_dev_destroy(rad_dev* d);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

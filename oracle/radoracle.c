@@ -466,6 +466,86 @@ static void shade(const tri_t *src, int logsrc, tri_t *des, int logdes) {
 }
 
 /* ---------------------------------------------------------------- init */
+/* Neighbour links, src/rad.cpp:295-334.  The reference compares every pair
+ * (i, j), j ascending, and later writes win.  Only pairs that share an exact
+ * vertex can write, so corners are bucketed by vertex and, for each i in
+ * ascending order, the writes are applied in the reference's (j, v, n) order:
+ * the final links equal those of the sequential O(N^2) scan. */
+typedef struct { uint64_t k[3]; int tri, v; } corner_t;
+static uint64_t coord_bits(real x) {
+    if (x == 0) return 0; /* +0 and -0 compare equal */
+    uint64_t b = 0;
+    memcpy(&b, &x, sizeof(real));
+    return b;
+}
+static int corner_cmp(const void *a, const void *b) {
+    const corner_t *x = a, *y = b;
+    for (int q = 0; q < 3; q++)
+        if (x->k[q] != y->k[q]) return x->k[q] < y->k[q] ? -1 : 1;
+    if (x->tri != y->tri) return x->tri < y->tri ? -1 : 1;
+    return x->v - y->v;
+}
+typedef struct { int j, v, n; } nbw_t;
+static int nbw_cmp(const void *a, const void *b) {
+    const nbw_t *x = a, *y = b;
+    if (x->j != y->j) return x->j < y->j ? -1 : 1;
+    if (x->v != y->v) return x->v - y->v;
+    return x->n - y->n;
+}
+static void link_neighbours(void) {
+    int n = trinum, m = 0;
+    corner_t *cs = malloc((size_t)(3 * n + 1) * sizeof(corner_t));
+    for (int i = 0; i < n; i++)
+        for (int v = 0; v < 3; v++) {
+            const real *p = T[i].p[v];
+            if (p[0] != p[0] || p[1] != p[1] || p[2] != p[2]) continue; /* NaN equals nothing */
+            for (int q = 0; q < 3; q++) cs[m].k[q] = coord_bits(p[q]);
+            cs[m].tri = i; cs[m].v = v; m++;
+        }
+    qsort(cs, (size_t)m, sizeof(corner_t), corner_cmp);
+    int *grp = malloc((size_t)(3 * n + 1) * sizeof(int)), *gs = malloc((size_t)(m + 2) * sizeof(int));
+    for (int q = 0; q < 3 * n; q++) grp[q] = -1;
+    int ng = 0;
+    for (int a = 0; a < m;) {
+        int b = a + 1;
+        while (b < m && !memcmp(cs[b].k, cs[a].k, sizeof cs[a].k)) b++;
+        gs[ng] = a;
+        for (int q = a; q < b; q++) grp[3 * cs[q].tri + cs[q].v] = ng;
+        ng++;
+        a = b;
+    }
+    gs[ng] = m;
+    int wcap = 64;
+    nbw_t *w = malloc((size_t)wcap * sizeof(nbw_t));
+    for (int i = 0; i < n; i++) {
+        int nw = 0;
+        for (int v = 0; v < 3; v++) {
+            int g = grp[3 * i + v];
+            if (g < 0) continue;
+            for (int q = gs[g]; q < gs[g + 1]; q++) {
+                if (cs[q].tri == i) continue;
+                if (nw == wcap) { wcap *= 2; w = realloc(w, (size_t)wcap * sizeof(nbw_t)); }
+                w[nw].j = cs[q].tri; w[nw].v = v; w[nw].n = cs[q].v; nw++;
+            }
+        }
+        qsort(w, (size_t)nw, sizeof(nbw_t), nbw_cmp);
+        tri_t *tp = &T[i];
+        for (int q = 0; q < nw; q++) {
+            int j = w[q].j, v = w[q].v, nn = w[q].n;
+            tri_t *tn = &T[j];
+            const real *a1 = tp->p[(v + 1) % 3], *b1 = tn->p[(nn + 1) % 3], *b2 = tn->p[(nn + 2) % 3];
+            real cs_ = dot3(tp->n, tn->n) / len3(tp->n) / len3(tn->n);
+            if (a1[0] == b1[0] && a1[1] == b1[1] && a1[2] == b1[2]) {
+                if ((double)cs_ > 0.85) { tp->nb[v] = j; tn->nb[nn] = i; }
+            } else if (a1[0] == b2[0] && a1[1] == b2[1] && a1[2] == b2[2]) {
+                if ((double)cs_ > 0.85) { tp->nb[v] = j; tn->nb[(nn + 2) % 3] = i; }
+            }
+        }
+    }
+    free(w); free(gs); free(grp); free(cs);
+}
+
+
 /* src/rad.cpp:259-356 */
 static void init_radiosity(void) {
     real minarea = 100000000.0, maxarea = 0.0;
@@ -484,24 +564,8 @@ static void init_radiosity(void) {
             memset(tp->accB, 0, sizeof(tp->accB));
             memset(tp->deltaB, 0, sizeof(tp->deltaB));
         }
-        /* neighbour search, rad.cpp:295-334, in the sequential (j ascending) order */
-        for (int j = 0; j < trinum; j++) {
-            if (j == i) continue;
-            tri_t *tn = &T[j];
-            for (int v = 0; v < 3; v++)
-                for (int n = 0; n < 3; n++) {
-                    const real *a = tp->p[v], *b = tn->p[n];
-                    if (!(a[0] == b[0] && a[1] == b[1] && a[2] == b[2])) continue;
-                    const real *a1 = tp->p[(v + 1) % 3], *b1 = tn->p[(n + 1) % 3], *b2 = tn->p[(n + 2) % 3];
-                    real cs = dot3(tp->n, tn->n) / len3(tp->n) / len3(tn->n);
-                    if (a1[0] == b1[0] && a1[1] == b1[1] && a1[2] == b1[2]) {
-                        if ((double)cs > 0.85) { tp->nb[v] = j; tn->nb[n] = i; }
-                    } else if (a1[0] == b2[0] && a1[1] == b2[1] && a1[2] == b2[2]) {
-                        if ((double)cs > 0.85) { tp->nb[v] = j; tn->nb[(n + 2) % 3] = i; }
-                    }
-                }
-        }
     }
+    link_neighbours();
     if (SampleArea < 0.0) SampleArea = (float)((double)maxarea / 100.0);
     printf("[INFO] Max Patch Area = %f\n", (double)maxarea);
     printf("[INFO] Min Patch Area = %f\n", (double)minarea);
@@ -910,6 +974,54 @@ static void put_dump(const char *path, int steps) {
     fclose(f);
 }
 
+/* ---------------------------------------------------------------- queries */
+/* RAD_RAYS=path: binary input of n records {real p[3], real v[3], int32 ban}
+ * (after pre-partition); writes path.out with one int32 RayHitted result per
+ * record.  RAD_FF=path: input int32 src, int32 n, int32 rcv[n]; writes
+ * path.out with real ff[n][3] = AdaptCalFF(CalFF(...)) per receiver corner. */
+static void run_queries(void) {
+    const char *rp = getenv("RAD_RAYS");
+    if (rp) {
+        FILE *f = fopen(rp, "rb");
+        char op[4096];
+        snprintf(op, sizeof op, "%s.out", rp);
+        FILE *g = fopen(op, "wb");
+        if (f && g) {
+            real pv[6];
+            int ban;
+            while (fread(pv, sizeof(real), 6, f) == 6 && fread(&ban, 4, 1, f) == 1) {
+                int hit = ray_hit(pv, pv + 3, ban, -1);
+                fwrite(&hit, 4, 1, g);
+            }
+        }
+        if (f) fclose(f);
+        if (g) fclose(g);
+    }
+    const char *fp = getenv("RAD_FF");
+    if (fp) {
+        FILE *f = fopen(fp, "rb");
+        char op[4096];
+        snprintf(op, sizeof op, "%s.out", fp);
+        FILE *g = fopen(op, "wb");
+        int src, n;
+        if (f && g && fread(&src, 4, 1, f) == 1 && fread(&n, 4, 1, f) == 1) {
+            patch_t sp;
+            as_patch(&T[src], &sp);
+            for (int k = 0; k < n; k++) {
+                int r;
+                if (fread(&r, 4, 1, f) != 1) break;
+                real ff[3];
+                for (int v = 0; v < 3; v++)
+                    ff[v] = adapt_ff(point_ff(&sp, T[src].parent, &T[r], T[r].parent, T[r].p[v]), &sp, T[src].parent,
+                                     &T[r], T[r].parent, T[r].p[v]);
+                fwrite(ff, sizeof(real), 3, g);
+            }
+        }
+        if (f) fclose(f);
+        if (g) fclose(g);
+    }
+}
+
 /* ---------------------------------------------------------------- main */
 static double now_s(void) {
     struct timespec ts;
@@ -964,6 +1076,7 @@ int main(int argc, char **argv) {
 
     init_radiosity();
     pre_partition();
+    run_queries();
     double t2 = now_s();
     int loop, steps = 0;
     for (loop = 1;; loop++) {
