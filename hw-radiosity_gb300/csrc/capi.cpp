@@ -212,6 +212,21 @@ int rad_octree_info(const rad_octree* t, int64_t* ref_nodes, int64_t* ref_list, 
     return RAD_OK;
 }
 
+int rad_octree_cell_coords(const rad_octree* t, int32_t axis, const void* q, int32_t n, int32_t* out_ref,
+                           int32_t* out_fast) {
+    if (!t || axis < 0 || axis > 2 || (n > 0 && (!q || !out_ref || !out_fast)))
+        return fail(RAD_ERR_ARG, "rad_octree_cell_coords: bad argument");
+    auto go = [&](auto& o, auto* qq) {
+        for (int32_t i = 0; i < n; i++) {
+            out_ref[i] = cell_coord(qq[i], o.G0[axis], o.min_grid);
+            out_fast[i] = cell_of_thresholds(o, axis, qq[i]);
+        }
+    };
+    if (t->precision == 32) go(t->o32, (const float*)q);
+    else go(t->o64, (const double*)q);
+    return RAD_OK;
+}
+
 void rad_octree_free(rad_octree* t) { delete t; }
 
 }  // extern "C"

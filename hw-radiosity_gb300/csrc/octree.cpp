@@ -15,7 +15,9 @@
 // triangle id, as every list is a filtered copy of 0..n-1).
 #include <algorithm>
 #include <atomic>
+#include <cmath>
 #include <cstring>
+#include <limits>
 #include <future>
 #include <thread>
 
@@ -78,6 +80,31 @@ bool tri_meets_box(const T (*p)[3], const T* g0, const T* g1) {
 }
 
 struct Node { int32_t child[8]; int32_t leaf; };
+
+// order-preserving unsigned image of a float / double
+template <typename T> struct OrderedBits;
+template <> struct OrderedBits<float> {
+    static uint32_t to(float x) {
+        uint32_t b; std::memcpy(&b, &x, 4);
+        return (b >> 31) ? ~b : (b | 0x80000000u);
+    }
+    static float from(uint32_t o) {
+        uint32_t b = (o >> 31) ? (o & 0x7fffffffu) : ~o;
+        float x; std::memcpy(&x, &b, 4);
+        return x;
+    }
+};
+template <> struct OrderedBits<double> {
+    static uint64_t to(double x) {
+        uint64_t b; std::memcpy(&b, &x, 8);
+        return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+    }
+    static double from(uint64_t o) {
+        uint64_t b = (o >> 63) ? (o & 0x7fffffffffffffffull) : ~o;
+        double x; std::memcpy(&x, &b, 8);
+        return x;
+    }
+};
 
 template <typename T>
 struct Part {                      // one independently built subtree
@@ -207,8 +234,35 @@ void build_octree(const Scene<T>& s, Octree<T>& o, int threads) {
     }
     o.entry_tri = std::move(P.entries);
 
-    // cell table: leaf of every cell-coordinate triple (TreeNodeNum's descent)
     for (int a = 0; a < 3; a++) o.dims[a] = cell_coord<T>(s.G1[a], s.G0[a], o.min_grid) + 1;
+    // exact cell-coordinate thresholds per axis (binary search over the
+    // ordered bit patterns of T between G0 and G1)
+    o.thr.clear();
+    for (int a = 0; a < 3; a++) {
+        o.thr_off[a] = (int32_t)o.thr.size();
+        const int D = o.dims[a];
+        o.thr.push_back(s.G0[a]);
+        for (int k = 1; k < D; k++) {
+            auto lo = OrderedBits<T>::to(s.G0[a]), hi = OrderedBits<T>::to(s.G1[a]);
+            while (lo < hi) {
+                auto mid = lo + (hi - lo) / 2;
+                if (cell_coord<T>(OrderedBits<T>::from(mid), s.G0[a], o.min_grid) >= k) hi = mid;
+                else lo = mid + 1;
+            }
+            o.thr.push_back(OrderedBits<T>::from(lo));
+        }
+        o.thr.push_back(std::numeric_limits<T>::infinity());
+    }
+    {
+        T c = (T)0.0001;
+        if ((double)c < 0.0001) c = std::nextafter(c, std::numeric_limits<T>::infinity());
+        o.t_eps = c;
+        T d = (T)1e-6;
+        if ((double)d > 1e-6) d = std::nextafter(d, -std::numeric_limits<T>::infinity());
+        o.v_eps = d;
+    }
+
+    // cell table: leaf of every cell-coordinate triple (TreeNodeNum's descent)
     const size_t ncell = (size_t)o.dims[0] * o.dims[1] * o.dims[2];
     o.cell_leaf.assign(ncell, -1);
     for (int gx = 0; gx < o.dims[0]; gx++)
@@ -228,6 +282,31 @@ void build_octree(const Scene<T>& s, Octree<T>& o, int threads) {
             }
 }
 
+template <typename T>
+int cell_of_thresholds(const Octree<T>& o, int a, T q) {
+    const T* th = o.thr.data() + o.thr_off[a];
+    const int D = o.dims[a];
+    int k = (int)((q - o.G0[a]) * (T)(1.0 / (double)o.min_grid));
+    k = std::min(std::max(k, 0), D - 1);
+    while (k + 1 < D && q >= th[k + 1]) ++k;
+    while (k > 0 && q < th[k]) --k;
+    return k;
+}
+
+template <typename T>
+bool thresholds_consistent(const Octree<T>& o) {
+    size_t need = 0;
+    for (int a = 0; a < 3; a++) {
+        if (o.dims[a] < 1 || o.thr_off[a] != (int32_t)need) return false;
+        need += (size_t)o.dims[a] + 1;
+    }
+    return need == o.thr.size();
+}
+
+template int cell_of_thresholds<float>(const Octree<float>&, int, float);
+template int cell_of_thresholds<double>(const Octree<double>&, int, double);
+template bool thresholds_consistent<float>(const Octree<float>&);
+template bool thresholds_consistent<double>(const Octree<double>&);
 template void build_octree<float>(const Scene<float>&, Octree<float>&, int);
 template void build_octree<double>(const Scene<double>&, Octree<double>&, int);
 

@@ -84,8 +84,12 @@ __device__ __forceinline__ unsigned long long key_order(double f) {
 template <typename T>
 struct Grid {
     T g0[3], g1[3];
-    T min_grid;
+    T inv_grid;                              // 1 / MinGridLen, for the first guess only
+    T t_eps, v_eps;                          // exact FP32 images of the 0.0001 and 1e-6 tests
     int dims[3];
+    int thr_off[3];
+    int n_thr;
+    const T* thr;                            // cell-coordinate thresholds (global; staged to smem)
     const int32_t* __restrict__ cell_leaf;   // cell coordinate triple -> leaf
     const Q4<T>* __restrict__ leaf;          // 2 per leaf: (g0, begin) (g1, end)
     const Q4<T>* __restrict__ entry;         // 5 per list entry: (n, id) (c, 0) se0 se1 se2
@@ -119,7 +123,14 @@ struct Shooter {
 
 struct Partial { unsigned long long key; int slot; int pad; };
 
+// dynamic shared memory of k_shoot: shooter records, then the thresholds
+template <typename T>
+__host__ __device__ inline size_t kMaxShooterBytes(int nsh) {
+    return ((size_t)nsh * sizeof(Shooter<T>) + 15) & ~(size_t)15;
+}
+
 struct State {
+    int work;               // next 10-slot group of the current step (k_shoot queue)
     int done;               // a selection found no candidate
     int paused;             // step limit reached
     int nsh;                // shooters of the current step
@@ -133,6 +144,17 @@ struct State {
 
 struct Cnt { unsigned rays, rays_ref, cells, tris, se, prec, capped; };
 
+// Cell coordinate along one axis: a first guess in T, corrected against the
+// thresholds so the result equals the reference's FP64 expression exactly.
+template <typename T>
+__device__ __forceinline__ int cell_axis(T q, T g0, T inv, const T* th, int D) {
+    int k = (int)((q - g0) * inv);
+    k = min(max(k, 0), D - 1);
+    while (k + 1 < D && q >= th[k + 1]) ++k;
+    while (k > 0 && q < th[k]) --k;
+    return k;
+}
+
 // ------------------------------------------------------------------ walk
 // RayHitted (raycast.cpp:335-360) with TreeNodeNum (254-281) as a table
 // lookup, TriListHitted/TriHitted (283-333) and NextPoint (235-251).
@@ -145,12 +167,10 @@ __device__ __forceinline__ int walk(const Grid<T>& G, const T p[3], const T v[3]
         if (q0 < G.g0[0] || q0 > G.g1[0] || q1 < G.g0[1] || q1 > G.g1[1] || q2 < G.g0[2] || q2 > G.g1[2])
             return -1;
         if (COUNT) c.cells++;
-        int gx = (int)(((double)q0 - (double)G.g0[0]) / (double)G.min_grid);
-        int gy = (int)(((double)q1 - (double)G.g0[1]) / (double)G.min_grid);
-        int gz = (int)(((double)q2 - (double)G.g0[2]) / (double)G.min_grid);
-        gx = min(max(gx, 0), G.dims[0] - 1);   // no-ops for points inside [G0, G1]
-        gy = min(max(gy, 0), G.dims[1] - 1);
-        gz = min(max(gz, 0), G.dims[2] - 1);
+        // (int)(((double)q - G0) / MinGridLen) per axis, found exactly from the thresholds
+        const int gx = cell_axis(q0, G.g0[0], G.inv_grid, G.thr + G.thr_off[0], G.dims[0]);
+        const int gy = cell_axis(q1, G.g0[1], G.inv_grid, G.thr + G.thr_off[1], G.dims[1]);
+        const int gz = cell_axis(q2, G.g0[2], G.inv_grid, G.thr + G.thr_off[2], G.dims[2]);
         const int leaf = __ldg(&G.cell_leaf[(gx * G.dims[1] + gy) * G.dims[2] + gz]);
         if (leaf == prev) {          // "Precision Exceeded": step one unit of t
             if (COUNT) c.prec++;
@@ -172,7 +192,7 @@ __device__ __forceinline__ int walk(const Grid<T>& G, const T p[3], const T v[3]
             const T w0 = ec.x - p[0], w1 = ec.y - p[1], w2 = ec.z - p[2];
             const T a2 = w0 * en.x + w1 * en.y + w2 * en.z;
             const T tt = a2 / a1;
-            if ((double)tt < 0.0001) continue;
+            if (tt < G.t_eps) continue;            // (double)t < 0.0001
             if (tt >= tmin) continue;
             if (COUNT) c.se++;
             const T x = p[0] + tt * v[0], y = p[1] + tt * v[1], z = p[2] + tt * v[2];
@@ -192,7 +212,7 @@ __device__ __forceinline__ int walk(const Grid<T>& G, const T p[3], const T v[3]
         T tm = (T)1000000.0;
 #pragma unroll
         for (int a = 0; a < 3; a++) {
-            if (fabs((double)v[a]) > 1e-6) {
+            if (fabs(v[a]) > G.v_eps) {             // fabs((double)v) > 1e-6
                 const T s = (v[a] > 0) ? (bh[a] - p[a]) / v[a] : (bl[a] - p[a]) / v[a];
                 tm = (s < tm) ? s : tm;
             }
@@ -279,26 +299,12 @@ __device__ __forceinline__ void flush_counters(State* st, Cnt& c, int lane) {
 }
 
 // ------------------------------------------------------------------ k_shoot
+// One 10-slot group: lanes 3r+v are corner v of slot g*10+r.
 template <typename T, bool COUNT>
-__global__ void __launch_bounds__(kShootThreads)
-k_shoot(Slots<T> S, Grid<T> G, const Shooter<T>* __restrict__ shooters, State* st, Partial* __restrict__ part, T conv) {
-    extern __shared__ __align__(16) unsigned char smem[];
-    Shooter<T>* sh = reinterpret_cast<Shooter<T>*>(smem);
-    __shared__ unsigned long long wkey[kShootThreads / 32];
-    __shared__ int wslot[kShootThreads / 32];
-    if (st->done || st->paused) return;
-    const int nsh = st->nsh;
-    {
-        const int words = nsh * (int)(sizeof(Shooter<T>) / 4);
-        const int* srcw = reinterpret_cast<const int*>(shooters);
-        int* dstw = reinterpret_cast<int*>(smem);
-        for (int k = threadIdx.x; k < words; k += blockDim.x) dstw[k] = srcw[k];
-    }
-    __syncthreads();
-
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+__device__ __forceinline__ void shoot_group(const Slots<T>& S, const Grid<T>& G, const Shooter<T>* sh, int nsh,
+                                            int g, int lane, T conv, unsigned long long& kk, int& ks, Cnt& c) {
     const int r = lane / 3, v = lane - 3 * r;
-    const int i = blockIdx.x * kSlotsPerCta + wid * kSlotsPerWarp + r;
+    const int i = g * kSlotsPerWarp + r;
     const bool own = lane < 3 * kSlotsPerWarp && i < S.n;
 
     Q4<T> fr = {0, 0, 0, (T)-1}, acc = {0, 0, 0, 0}, db = {0, 0, 0, 0};
@@ -311,13 +317,13 @@ k_shoot(Slots<T> S, Grid<T> G, const Shooter<T>* __restrict__ shooters, State* s
     bool is_src = false;
     for (int j = 0; j < nsh; j++) is_src |= (sh[j].slot == i);
     // a receiver is skipped only when all nine accB components are >= 255
-    const bool open_v = live && ((double)acc.x < 255.0 || (double)acc.y < 255.0 || (double)acc.z < 255.0);
+    const bool open_v = live && (acc.x < (T)255 || acc.y < (T)255 || acc.z < (T)255);
     const unsigned ballot = __ballot_sync(kFull, open_v);
-    const bool open = ((ballot >> (3 * min(r, 9))) & 7u) != 0;
+    const int base = 3 * min(r, kSlotsPerWarp - 1);
+    const bool open = ((ballot >> base) & 7u) != 0;
     const bool active = live && !is_src && open && nsh > 0;
     if (live && v == 0) db = S.deltaB[i];
 
-    Cnt c = {0, 0, 0, 0, 0, 0, 0};
     T pv[3] = {0, 0, 0}, nd[3] = {0, 0, 0}, ndlen = 1;
     if (active) {
         const Q4<T> pp = S.vtx[i * 3 + v];
@@ -332,7 +338,6 @@ k_shoot(Slots<T> S, Grid<T> G, const Shooter<T>* __restrict__ shooters, State* s
     for (int j = 0; j < nsh; j++) {
         T ff = 0;
         if (active) ff = corner_ff<T, COUNT>(sh[j], pv, nd, ndlen, parent, G, c);
-        const int base = 3 * min(r, 9);
         const T f0 = shfl(ff, base), f1 = shfl(ff, base + 1), f2 = shfl(ff, base + 2);
         if (active) {
             const T lo0 = fr.x * k * sh[j].deltaB[0] / 3;
@@ -357,21 +362,68 @@ k_shoot(Slots<T> S, Grid<T> G, const Shooter<T>* __restrict__ shooters, State* s
         S.deltaB[i] = q;
     }
     // next selection: key = (dB0 + dB1) + dB2 (rad.cpp:394), candidates > converge
-    unsigned long long kk = 0;
-    int ks = -1;
     if (live && v == 0) {
         const T key = (d0 + d1) + d2;
-        if (key > conv) { kk = key_order(key); ks = i; }
+        if (key > conv) {
+            const unsigned long long o = key_order(key);
+            if (part_less(kk, ks, o, i)) { kk = o; ks = i; }
+        }
+    }
+}
+
+// Persistent: each warp takes 10-slot groups from the step's queue until it
+// is empty, so warps that finish early take more work; the CTA's (key, slot)
+// maximum is written by whichever of its warps finishes last.
+template <typename T, bool COUNT>
+__global__ void __launch_bounds__(kShootThreads)
+k_shoot(Slots<T> S, Grid<T> G, const Shooter<T>* __restrict__ shooters, State* st, Partial* __restrict__ part, T conv) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ unsigned long long wkey[kShootThreads / 32];
+    __shared__ int wslot[kShootThreads / 32];
+    __shared__ int ndone;
+    if (st->done || st->paused) return;
+    const int nsh = st->nsh;
+    Shooter<T>* sh = reinterpret_cast<Shooter<T>*>(smem);
+    T* thr = reinterpret_cast<T*>(smem + kMaxShooterBytes<T>(nsh));
+    {
+        const int words = nsh * (int)(sizeof(Shooter<T>) / 4);
+        const int* srcw = reinterpret_cast<const int*>(shooters);
+        int* dstw = reinterpret_cast<int*>(smem);
+        for (int q = threadIdx.x; q < words; q += blockDim.x) dstw[q] = srcw[q];
+        for (int q = threadIdx.x; q < G.n_thr; q += blockDim.x) thr[q] = G.thr[q];
+        if (threadIdx.x == 0) ndone = 0;
+    }
+    __syncthreads();
+    Grid<T> Gs = G;
+    Gs.thr = thr;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int n_groups = (S.n + kSlotsPerWarp - 1) / kSlotsPerWarp;
+    unsigned long long kk = 0;
+    int ks = -1;
+    Cnt c = {0, 0, 0, 0, 0, 0, 0};
+    for (;;) {
+        int g = 0;
+        if (lane == 0) g = atomicAdd(&st->work, 1);
+        g = __shfl_sync(kFull, g, 0);
+        if (g >= n_groups) break;
+        shoot_group<T, COUNT>(S, Gs, sh, nsh, g, lane, conv, kk, ks, c);
     }
     warp_max(kk, ks);
-    if (lane == 0) { wkey[wid] = kk; wslot[wid] = ks; }
     flush_counters<COUNT>(st, c, lane);
-    __syncthreads();
-    if (wid == 0) {
-        kk = lane < kShootThreads / 32 ? wkey[lane] : 0ull;
-        ks = lane < kShootThreads / 32 ? wslot[lane] : -1;
-        warp_max(kk, ks);
-        if (lane == 0) { part[blockIdx.x].key = kk; part[blockIdx.x].slot = ks; }
+    if (lane == 0) {
+        wkey[wid] = kk;
+        wslot[wid] = ks;
+        __threadfence_block();
+        if (atomicAdd(&ndone, 1) == kShootThreads / 32 - 1) {
+            volatile unsigned long long* vk = wkey;
+            volatile int* vs = wslot;
+            unsigned long long bk = 0;
+            int bs = -1;
+            for (int w = 0; w < kShootThreads / 32; w++)
+                if (part_less(bk, bs, vk[w], vs[w])) { bk = vk[w]; bs = vs[w]; }
+            part[blockIdx.x].key = bk;
+            part[blockIdx.x].slot = bs;
+        }
     }
 }
 
@@ -504,6 +556,7 @@ k_setup(Slots<T> S, Shooter<T>* shooters, State* st, const Partial* __restrict__
         for (int j = 0; j < P; j++)
             if (base + j < st->trace_cap) st->trace[base + j] = j < n ? chosen[j] : -1;
         st->nsh = n;
+        st->work = 0;
         st->steps += 1;
     }
 }
@@ -604,7 +657,8 @@ struct DevImpl : DevBase {
         *p = (U*)q;
         return RAD_OK;
     }
-    size_t shoot_smem() const { return (size_t)P * sizeof(Shooter<T>); }
+    int n_thr = 0;
+    size_t shoot_smem() const { return kMaxShooterBytes<T>(P) + (size_t)n_thr * sizeof(T); }
 };
 
 template <typename T>
@@ -644,6 +698,7 @@ int upload(const Scene<T>& s, const Octree<T>& o, const rad_options& opt, int de
     CU(cudaMemcpyAsync(d_db, db.data(), db.size() * sizeof(Q4<T>), cudaMemcpyHostToDevice, d.stream));
     d.S = Slots<T>{n, d_vtx, d_nrm, d_ctr, d_frgb, d_acc, d_db};
 
+    if (!thresholds_consistent(o)) return fail(RAD_ERR_ARG, "octree cell thresholds do not match its dimensions");
     // visibility structure; the walk's triangle records come from the current slots
     const int n_leaves = (int)(o.leaf_range.size() / 2);
     const size_t n_ent = o.entry_tri.size();
@@ -668,17 +723,38 @@ int upload(const Scene<T>& s, const Octree<T>& o, const rad_options& opt, int de
     CU(cudaMemcpyAsync(d_leaf, leaf.data(), leaf.size() * sizeof(Q4<T>), cudaMemcpyHostToDevice, d.stream));
     CU(cudaMemcpyAsync(d_ent, ent.data(), ent.size() * sizeof(Q4<T>), cudaMemcpyHostToDevice, d.stream));
     CU(cudaMemcpyAsync(d_cell, o.cell_leaf.data(), o.cell_leaf.size() * 4, cudaMemcpyHostToDevice, d.stream));
+    T* d_thr;
+    if ((rc = d.alloc(&d_thr, o.thr.size()))) return rc;
+    CU(cudaMemcpyAsync(d_thr, o.thr.data(), o.thr.size() * sizeof(T), cudaMemcpyHostToDevice, d.stream));
     Grid<T> G{};
-    for (int k = 0; k < 3; k++) { G.g0[k] = o.G0[k]; G.g1[k] = o.G1[k]; G.dims[k] = o.dims[k]; }
-    G.min_grid = o.min_grid;
+    for (int k = 0; k < 3; k++) {
+        G.g0[k] = o.G0[k]; G.g1[k] = o.G1[k]; G.dims[k] = o.dims[k]; G.thr_off[k] = o.thr_off[k];
+    }
+    G.inv_grid = (T)(1.0 / (double)o.min_grid);
+    G.t_eps = o.t_eps;
+    G.v_eps = o.v_eps;
+    G.n_thr = (int)o.thr.size();
+    G.thr = d_thr;
     G.cell_leaf = d_cell;
     G.leaf = d_leaf;
     G.entry = d_ent;
     G.walk_cap = opt.walk_cap > 0 ? opt.walk_cap : (1 << 20);
     d.G = G;
 
-    // per-step state
-    d.n_cta = std::max(1, (n + kSlotsPerCta - 1) / kSlotsPerCta);
+    // per-step state; k_shoot is persistent: as many CTAs as fit at once
+    d.n_thr = (int)o.thr.size();
+    if (d.shoot_smem() > 48 * 1024) {
+        CU(cudaFuncSetAttribute(k_shoot<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)d.shoot_smem()));
+        CU(cudaFuncSetAttribute(k_shoot<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)d.shoot_smem()));
+    }
+    {
+        int sms = 0, per_sm = 0;
+        CU(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+        CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_shoot<T, false>, kShootThreads, d.shoot_smem()));
+        const int n_groups = (n + kSlotsPerWarp - 1) / kSlotsPerWarp;
+        const int want = (n_groups + kShootThreads / 32 - 1) / (kShootThreads / 32);
+        d.n_cta = std::max(1, std::min(want, std::max(1, sms * per_sm)));
+    }
     if ((rc = d.alloc(&d.d_shooters, (size_t)d.P)) || (rc = d.alloc(&d.d_state, 1)) ||
         (rc = d.alloc(&d.d_part, (size_t)d.n_cta)))
         return rc;
@@ -691,10 +767,6 @@ int upload(const Scene<T>& s, const Octree<T>& o, const rad_options& opt, int de
     CU(cudaMemcpyAsync(d.d_state, &st, sizeof st, cudaMemcpyHostToDevice, d.stream));
     CU(cudaMemsetAsync(d.d_shooters, 0, sizeof(Shooter<T>) * d.P, d.stream));
     CU(cudaMemsetAsync(d.d_part, 0, sizeof(Partial) * d.n_cta, d.stream));
-    if (d.shoot_smem() > 48 * 1024) {
-        CU(cudaFuncSetAttribute(k_shoot<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)d.shoot_smem()));
-        CU(cudaFuncSetAttribute(k_shoot<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)d.shoot_smem()));
-    }
     // initial selection keys: a step with no shooter only reduces the keys
     k_shoot<T, false><<<d.n_cta, kShootThreads, d.shoot_smem(), d.stream>>>(d.S, d.G, d.d_shooters, d.d_state, d.d_part, d.conv);
     CU(cudaGetLastError());

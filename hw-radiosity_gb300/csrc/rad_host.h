@@ -62,6 +62,14 @@ struct Octree {
     int32_t grid_num = 0;         // raycast.cpp:230
     int32_t dims[3] = {0, 0, 0};  // cell-table extent per axis (max cell coordinate + 1)
     std::vector<int32_t> cell_leaf;     // dims[0]*dims[1]*dims[2] -> leaf id
+    // thr[off[a] + k] = the smallest value q with cell_coord(q) >= k on axis a
+    // (k = 1..dims[a]-1; entries 0 and dims[a] are unused sentinels).  Cell
+    // coordinates are monotone in q, so k = #{thresholds <= q}: the device
+    // finds it exactly without the reference's FP64 division.
+    std::vector<T> thr;
+    int32_t thr_off[3] = {0, 0, 0};
+    T t_eps = 0;   // smallest T >= 0.0001: (double)t < 0.0001  <=>  t < t_eps
+    T v_eps = 0;   // largest T <= 1e-6:    fabs((double)v) > 1e-6  <=>  fabs(v) > v_eps
     std::vector<T> leaf_box;            // 8 per leaf: g0.xyz, 0, g1.xyz, 0
     std::vector<int32_t> leaf_range;    // 2 per leaf: [begin, end) into entry_tri
     std::vector<int32_t> entry_tri;     // triangle id per list entry
@@ -77,6 +85,11 @@ template <typename T> void init_radiosity(Scene<T>& s);              // src/rad.
 template <typename T> void prepartition(Scene<T>& s);                // src/shade.cpp:556-598
 template <typename T> int write_fin(const Scene<T>& s, const char* prefix, int loop, std::string& err);
 template <typename T> void build_octree(const Scene<T>& s, Octree<T>& o, int threads);  // raycast.cpp:216-233
+
+// The threshold method the device uses for cell coordinates, on the host
+// (tests compare it with cell_coord), and the size check run before upload.
+template <typename T> int cell_of_thresholds(const Octree<T>& o, int axis, T q);
+template <typename T> bool thresholds_consistent(const Octree<T>& o);
 
 // Cell coordinate along one axis, raycast.cpp:263 (shared with the device).
 template <typename T>

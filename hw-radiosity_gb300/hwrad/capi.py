@@ -23,7 +23,7 @@ EXPORTS = [
     "rad_options_default", "rad_last_error", "rad_version",
     "rad_scene_load", "rad_scene_from_arrays", "rad_scene_init", "rad_scene_prepartition",
     "rad_scene_view_get", "rad_scene_write_fin", "rad_scene_log", "rad_scene_free",
-    "rad_octree_build", "rad_octree_info", "rad_octree_free",
+    "rad_octree_build", "rad_octree_info", "rad_octree_cell_coords", "rad_octree_free",
     "rad_dev_create", "rad_dev_run", "rad_dev_run_timed", "rad_dev_run_profiled", "rad_dev_download", "rad_dev_trace", "rad_dev_stats",
     "rad_dev_set_counting", "rad_dev_ray_hit", "rad_dev_form_factors", "rad_dev_destroy",
 ]
@@ -90,6 +90,7 @@ def load(path: Optional[str] = None) -> C.CDLL:
         "rad_scene_free": (None, [vp]),
         "rad_octree_build": (C.c_int, [vp, i32, P(vp)]),
         "rad_octree_info": (C.c_int, [vp, P(i64), P(i64), P(i32), P(i64), P(i32)]),
+        "rad_octree_cell_coords": (C.c_int, [vp, i32, vp, i32, vp, vp]),
         "rad_octree_free": (None, [vp]),
         "rad_dev_create": (C.c_int, [vp, vp, P(Options), i32, P(vp)]),
         "rad_dev_run": (C.c_int, [vp, i64, P(i64), P(i32)]),
@@ -228,6 +229,14 @@ class Octree:
         _check(load().rad_octree_info(self.h, C.byref(a), C.byref(b), C.byref(nl), C.byref(e), dims))
         return {"ref_nodes": a.value, "ref_list": b.value, "leaves": nl.value, "entries": e.value,
                 "dims": list(dims)}
+
+    def cell_coords(self, axis: int, q: np.ndarray, dtype=np.float32):
+        """(reference expression, device threshold method) cell coordinates of q."""
+        q = np.ascontiguousarray(q, dtype)
+        a = np.zeros(len(q), np.int32)
+        b = np.zeros(len(q), np.int32)
+        _check(load().rad_octree_cell_coords(self.h, axis, q.ctypes.data, len(q), a.ctypes.data, b.ctypes.data))
+        return a, b
 
     def close(self):
         if self.h:

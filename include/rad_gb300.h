@@ -131,6 +131,12 @@ void rad_scene_free(rad_scene* s);
 int rad_octree_build(const rad_scene* s, int32_t threads, rad_octree** out);
 int rad_octree_info(const rad_octree* t, int64_t* ref_nodes, int64_t* ref_list, int32_t* n_leaves,
                     int64_t* n_entries, int32_t dims[3]);
+/* Cell coordinates of points q[n] (float or double per the octree's
+ * precision) on one axis, two ways: out_ref by the reference's expression
+ * (int)(((double)q - G0) / MinGridLen) (raycast.cpp:263), out_fast by the
+ * threshold search the device uses.  They are equal for q inside [G0, G1]. */
+int rad_octree_cell_coords(const rad_octree* t, int32_t axis, const void* q, int32_t n, int32_t* out_ref,
+                           int32_t* out_fast);
 void rad_octree_free(rad_octree* t);
 
 /* ---- device solver ------------------------------------------------------ */

@@ -105,3 +105,33 @@ def test_trailing_token_without_newline(built, workdir):
     with open(p, "w") as fh:
         fh.write(text)
     assert capi.Scene.load(p, capi.options()).view()["n"] == s.n
+
+
+@pytest.mark.parametrize("fp64", [False, True])
+def test_cell_thresholds_equal_reference_expression(built, workdir, fp64):
+    """The device finds (int)(((double)q - G0) / MinGridLen) from per-axis
+    thresholds; on the host the same search must agree with the expression for
+    every q in [G0, G1], including values next to each threshold."""
+    ft = np.float64 if fp64 else np.float32
+    for q_, size in ((8, 10.0), (64, 10.0), (3, 40.0)):
+        s = scenes.room_with_boxes(q_, 4, 1, seed=q_, size=size)
+        tri = s.write(os.path.join(workdir, f"thr{q_}.tri"))
+        sc = capi.Scene.load(tri, capi.options(precision=64 if fp64 else 32))
+        tree = capi.Octree(sc, 2)
+        v = sc.view()
+        rng = np.random.default_rng(q_)
+        for axis in range(3):
+            g0, g1 = ft(v["G0"][axis]), ft(v["G1"][axis])
+            if fp64:   # the view reports corners as float; use the scene's own bounds
+                g0, g1 = ft(np.nextafter(g0, np.inf)), ft(np.nextafter(g1, -np.inf))
+            q = rng.uniform(g0, g1, 200000).astype(ft)
+            ref, fast = tree.cell_coords(axis, q, ft)
+            # neighbours of every cell boundary the sample found
+            edges = q[np.nonzero(np.diff(ref[np.argsort(q)]))[0]]
+            near = np.concatenate([np.nextafter(edges, -np.inf), edges, np.nextafter(edges, np.inf),
+                                   np.nextafter(np.nextafter(edges, np.inf), np.inf)]).astype(ft)
+            near = near[(near >= g0) & (near <= g1)]
+            r2, f2 = tree.cell_coords(axis, near, ft)
+            assert np.array_equal(ref, fast)
+            assert np.array_equal(r2, f2)
+            assert ref.min() >= 0 and ref.max() <= tree.info()["dims"][axis] - 1
