@@ -31,6 +31,7 @@
 
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -595,6 +596,43 @@ __global__ void k_form_factors(Slots<T> S, Grid<T> G, const Shooter<T>* __restri
     if (c.capped) atomicAdd(&st->capped, (unsigned long long)c.capped);
 }
 
+// ------------------------------------------------------------------ no-allocation variant
+// Shooter records for rad_dev_form_factors_noalloc live in this fixed array
+// instead of memory allocated per call.  Sized for the FP64 record, so it
+// serves both precisions.
+constexpr int kNoAllocMaxShooters = 64;
+static __device__ __align__(256) unsigned char g_noalloc_shooters[kNoAllocMaxShooters * sizeof(Shooter<double>)];
+
+struct ShooterSlots { int slot[kNoAllocMaxShooters]; };
+
+template <typename T>
+__global__ void k_build_many(Slots<T> S, ShooterSlots src, int n_src, Shooter<T>* out) {
+    const int j = threadIdx.x;
+    if (j < n_src) build_shooter(S, src.slot[j], out[j]);
+}
+
+// ff[(s * n_rcv + i) * 3 + v] for shooter s, receiver rcv[i], corner v;
+// receivers outside [0, n_slots) give NaN
+template <typename T>
+__global__ void k_form_factors_many(Slots<T> S, Grid<T> G, const Shooter<T>* __restrict__ sh, int n_src,
+                                    const int* __restrict__ rcv, int n_rcv, T* __restrict__ ff, State* st) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    Cnt c = {0, 0, 0, 0, 0, 0, 0};
+    if (t < 3LL * n_rcv * n_src) {
+        const int s = (int)(t / (3LL * n_rcv));
+        const int rem = (int)(t - (long long)s * 3 * n_rcv);
+        const int i = rcv[rem / 3], v = rem % 3;
+        if (i < 0 || i >= S.n) {
+            ff[t] = (T)NAN;
+        } else {
+            const Q4<T> pp = S.vtx[i * 3 + v], nn = S.nrm[i], fr = S.frgb[i];
+            const T pv[3] = {pp.x, pp.y, pp.z}, nd[3] = {nn.x, nn.y, nn.z};
+            ff[t] = corner_ff<T, false>(sh[s], pv, nd, nn.w, (int)fr.w, G, c);
+        }
+    }
+    if (c.capped) atomicAdd(&st->capped, (unsigned long long)c.capped);
+}
+
 }  // namespace dev
 }  // namespace radgb
 
@@ -957,6 +995,56 @@ int form_factors(DevImpl<T>& d, int src, const int32_t* rcv, int n, T* ff) {
     return RAD_OK;
 }
 
+// Device address of g_noalloc_shooters, looked up once per device with that
+// device current (a host-side use of the symbol's name is not a device address).
+std::mutex g_noalloc_mu;
+void* g_noalloc_ptr[64] = {};
+
+int noalloc_scratch(int device, void** out) {
+    if (device < 0 || device >= 64) return fail(RAD_ERR_ARG, "device index out of range");
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_ptr[device]) {
+        int cur = 0;
+        CU(cudaGetDevice(&cur));
+        if (cur != device) CU(cudaSetDevice(device));
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_shooters);
+        if (cur != device) cudaSetDevice(cur);
+        if (e != cudaSuccess) return fail(RAD_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+        g_noalloc_ptr[device] = p;
+    }
+    *out = g_noalloc_ptr[device];
+    return RAD_OK;
+}
+
+template <typename T>
+int form_factors_noalloc(DevImpl<T>& d, const int32_t* src, int n_src, const int32_t* d_rcv, int n_rcv, T* d_ff,
+                         cudaStream_t stream) {
+    if (n_src < 1 || n_src > kNoAllocMaxShooters)
+        return fail(RAD_ERR_CAPACITY, "rad_dev_form_factors_noalloc: 1 to 64 shooters per call");
+    if (n_rcv < 0 || (n_rcv > 0 && (!d_rcv || !d_ff)) || !src)
+        return fail(RAD_ERR_ARG, "rad_dev_form_factors_noalloc: bad argument");
+    if ((long long)n_src * n_rcv * 3 > 0x7fffffffLL)
+        return fail(RAD_ERR_CAPACITY, "rad_dev_form_factors_noalloc: n_src * n_rcv * 3 exceeds 2^31-1");
+    ShooterSlots slots{};
+    for (int j = 0; j < n_src; j++) {
+        if (src[j] < 0 || src[j] >= d.S.n) return fail(RAD_ERR_ARG, "shooter slot out of range");
+        slots.slot[j] = src[j];
+    }
+    CU(cudaSetDevice(d.device));
+    void* scratch = nullptr;
+    int rc = noalloc_scratch(d.device, &scratch);
+    if (rc) return rc;
+    Shooter<T>* sh = reinterpret_cast<Shooter<T>*>(scratch);
+    k_build_many<T><<<1, kNoAllocMaxShooters, 0, stream>>>(d.S, slots, n_src, sh);
+    const long long work = 3LL * n_rcv * n_src;
+    if (work > 0)
+        k_form_factors_many<T><<<(unsigned)((work + 255) / 256), 256, 0, stream>>>(d.S, d.G, sh, n_src, d_rcv, n_rcv,
+                                                                                 d_ff, d.d_state);
+    CU(cudaGetLastError());
+    return RAD_OK;
+}
+
 }  // namespace
 
 struct rad_dev {
@@ -1097,6 +1185,14 @@ int rad_dev_ray_hit(rad_dev* h, const void* p, const void* v, const int32_t* ban
 int rad_dev_form_factors(rad_dev* h, int32_t src, const int32_t* rcv, int32_t n, void* ff) {
     if (!h || (n > 0 && (!rcv || !ff))) return fail(RAD_ERR_ARG, "rad_dev_form_factors: null argument");
     return h->d32 ? form_factors(*h->d32, src, rcv, n, (float*)ff) : form_factors(*h->d64, src, rcv, n, (double*)ff);
+}
+
+int rad_dev_form_factors_noalloc(rad_dev* h, const int32_t* src, int32_t n_src, const int32_t* d_rcv, int32_t n_rcv,
+                                 void* d_ff, void* stream) {
+    if (!h) return fail(RAD_ERR_ARG, "rad_dev_form_factors_noalloc: null handle");
+    cudaStream_t s = (cudaStream_t)stream;
+    return h->d32 ? form_factors_noalloc(*h->d32, src, n_src, d_rcv, n_rcv, (float*)d_ff, s)
+                  : form_factors_noalloc(*h->d64, src, n_src, d_rcv, n_rcv, (double*)d_ff, s);
 }
 
 void rad_dev_destroy(rad_dev* h) { delete h; }

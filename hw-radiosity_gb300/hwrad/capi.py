@@ -25,7 +25,8 @@ EXPORTS = [
     "rad_scene_view_get", "rad_scene_write_fin", "rad_scene_log", "rad_scene_free",
     "rad_octree_build", "rad_octree_info", "rad_octree_cell_coords", "rad_octree_free",
     "rad_dev_create", "rad_dev_run", "rad_dev_run_timed", "rad_dev_run_profiled", "rad_dev_download", "rad_dev_trace", "rad_dev_stats",
-    "rad_dev_set_counting", "rad_dev_ray_hit", "rad_dev_form_factors", "rad_dev_destroy",
+    "rad_dev_set_counting", "rad_dev_ray_hit", "rad_dev_form_factors", "rad_dev_form_factors_noalloc",
+    "rad_dev_destroy",
 ]
 
 
@@ -102,6 +103,7 @@ def load(path: Optional[str] = None) -> C.CDLL:
         "rad_dev_set_counting": (C.c_int, [vp, i32]),
         "rad_dev_ray_hit": (C.c_int, [vp, vp, vp, vp, i32, vp]),
         "rad_dev_form_factors": (C.c_int, [vp, i32, vp, i32, vp]),
+        "rad_dev_form_factors_noalloc": (C.c_int, [vp, vp, i32, vp, i32, vp, vp]),
         "rad_dev_destroy": (None, [vp]),
     }
     for name, (res, args) in sig.items():
@@ -311,6 +313,13 @@ class Device:
         out = np.zeros((len(rcv), 3), dtype)
         _check(load().rad_dev_form_factors(self.h, int(src), rcv.ctypes.data, len(rcv), out.ctypes.data))
         return out
+
+    def form_factors_noalloc(self, src, d_rcv: int, n_rcv: int, d_ff: int, stream: int = 0) -> int:
+        """Enqueue the allocation-free form factors on device buffers (raw
+        device pointers d_rcv, d_ff); returns the status code."""
+        src = np.ascontiguousarray(src, np.int32).reshape(-1)
+        return load().rad_dev_form_factors_noalloc(self.h, src.ctypes.data, len(src), C.c_void_p(d_rcv), n_rcv,
+                                                   C.c_void_p(d_ff), C.c_void_p(stream))
 
     def close(self):
         if self.h:

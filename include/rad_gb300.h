@@ -173,6 +173,31 @@ int rad_dev_ray_hit(rad_dev* d, const void* p, const void* v, const int32_t* ban
 /* Batched Shade form factors without deposit: ff[i*3+v] for receiver slot
  * rcv[i] from shooter slot src (AdaptCalFF(CalFF(...)), src/shade.cpp:442-450). */
 int rad_dev_form_factors(rad_dev* d, int32_t src, const int32_t* rcv, int32_t n, void* ff);
+/* Form factors without allocating: the variant of rad_dev_form_factors for
+ * callers that must not call cudaMalloc or cudaFree at this point -- code
+ * inside a CUDA graph capture it owns (an allocation would break the
+ * capture), a render or simulation loop with a fixed device-memory budget
+ * whose allocator owns all memory, or a real-time loop that cannot take an
+ * allocation's synchronisation.  No counterpart in the reference (its
+ * CalFF runs on host memory only).
+ *   src    host array of n_src shooter slots, 1 <= n_src <= 64
+ *   d_rcv  device array of n_rcv receiver slots (caller-allocated)
+ *   d_ff   device array of n_src * n_rcv * 3 reals (float, or double for a
+ *          precision-64 handle), caller-allocated; d_ff[(s*n_rcv + i)*3 + v]
+ *          is corner v of receiver d_rcv[i] seen from shooter src[s], as
+ *          rad_dev_form_factors computes it; a receiver slot outside the
+ *          scene gives NaN
+ *   stream cudaStream_t to enqueue on (NULL: the legacy default stream); the
+ *          call returns without synchronising
+ * The shooter records go to one fixed device array of 64 records (11 KB, held
+ * by every GPU that loads the library until exit) instead of allocated
+ * memory; more than 64 shooters is RAD_ERR_CAPACITY.  Every call reuses that
+ * array, so calls whose kernels can overlap on the GPU (different streams
+ * without ordering) race on it; order them on one stream.  The first call on
+ * each device looks the array's device address up (cudaGetSymbolAddress with
+ * that device current): make that first call before any stream capture. */
+int rad_dev_form_factors_noalloc(rad_dev* d, const int32_t* src, int32_t n_src, const int32_t* d_rcv, int32_t n_rcv,
+                                 void* d_ff, void* stream);
 void rad_dev_destroy(rad_dev* d);
 
 #ifdef __cplusplus
