@@ -43,6 +43,14 @@ BYTES_PER_TRI_TEST = 24
 BYTES_PER_SE_TEST = 48
 
 
+_T0 = time.time()
+
+
+def log(msg):
+    """Progress on stderr (the JSON line is the only stdout output)."""
+    print(f"[bench {time.time() - _T0:8.1f}s] {msg}", file=sys.stderr, flush=True)
+
+
 def _peaks():
     p = os.path.join(REPO, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -156,6 +164,58 @@ def cpu_reference(tri, argv, warmup, steps, prefer_ref=True):
             "seconds": b - a}
 
 
+def measure_batched(capi, n_scenes, warmup, iters, device):
+    """Config 4: n_scenes seeded rooms (triangles log-uniform in [500, 50000],
+    0-32 boxes), each converging at 1e-4 of its emitter key.  Batched: every
+    running scene does one shooter step per iteration, all in one launch.
+    Plain: the single-scene solver on each scene in turn, over the same
+    iterations.  Device time from CUDA events on each solver's stream."""
+    from hwrad import scenes as S
+    t0 = time.time()
+    gens = S.batch_rooms(n_scenes, seed=4000)
+    preps = []
+    for g in gens:
+        o = capi.options_from_argv(g.argv())
+        sc = capi.Scene.from_arrays(g.vtx, g.frgb, g.brgb, o)
+        tr = capi.Octree(sc, _nproc())
+        sc.init()
+        sc.prepartition()
+        preps.append((sc, tr, o))
+    prep_s = time.time() - t0
+    log(f"batch: {n_scenes} scenes prepared in {prep_s:.1f} s")
+    tris = [p[0].view()["n"] for p in preps]
+    b = capi.Batch([p[0] for p in preps], [p[1] for p in preps], [p[2] for p in preps], device)
+    b.run(warmup)
+    s0 = sum(b.scene_stats(i)[0] for i in range(n_scenes))
+    it, active, ms = b.run_timed(iters)
+    s1 = sum(b.scene_stats(i)[0] for i in range(n_scenes))
+    st = b.stats()
+    dev_bytes = st["device_bytes"]
+    b.close()
+    batched = (s1 - s0) / (ms / 1000.0) if ms > 0 else None
+    log(f"batch: {it} iterations, {s1 - s0} shots in {ms:.1f} ms")
+    plain_ms = 0.0
+    plain_shots = 0
+    for k, (sc, tr, o) in enumerate(preps):
+        if k % 32 == 0:
+            log(f"plain: scene {k}")
+        d = capi.Device(sc, tr, o, device)
+        d.run(warmup)
+        n, conv, m = d.run_timed(iters)
+        plain_ms += m
+        plain_shots += n
+        d.close()
+    plain = plain_shots / (plain_ms / 1000.0) if plain_ms > 0 else None
+    log(f"plain: {plain_shots} shots in {plain_ms:.1f} ms")
+    return {"workload": f"{n_scenes} rooms (config 4), {sum(tris):,} triangles, {min(tris)}-{max(tris)} per scene",
+            "iterations": it, "shots": s1 - s0, "active_scenes_end": active,
+            "batched_shots_per_s": batched, "plain_shots_per_s": plain,
+            "batched_over_plain": batched / plain if batched and plain else None,
+            "batched_ms_per_iter": ms / max(it, 1), "plain_shots": plain_shots,
+            "device_bytes": dev_bytes, "host_prep_s": round(prep_s, 1),
+            "l2": "batch inputs exceed L2; plain timed without flush (graph chunks)"}
+
+
 def run_reference_arm(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -182,7 +242,12 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--batch-scenes", type=int, default=256, help="0 skips the batched measurement")
+    ap.add_argument("--batch-iters", type=int, default=100)
     args = ap.parse_args()
+    if os.environ.get("RAD_BENCH_STALL_DUMP"):
+        import faulthandler
+        faulthandler.dump_traceback_later(float(os.environ["RAD_BENCH_STALL_DUMP"]), repeat=True, file=sys.stderr)
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
@@ -214,6 +279,7 @@ def main():
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         return float(t.item())
 
+    log("config-2 scene: host preparation")
     tmp = tempfile.mkdtemp(prefix="radbench_")
     sc_gen, tri = _scene_file(tmp)
     argv = sc_gen.argv()
@@ -254,6 +320,7 @@ def main():
     st_main = dev.stats()
     dev.close()
 
+    log(f"timed {done} steps: {total_ms:.2f} ms; steady state {n_ss} steps {ms_ss:.2f} ms")
     # ---- per-kernel durations over the same steps (fresh instance, one launch at a time)
     dprof = capi.Device(scene, tree, opts, local)
     dprof.run(args.warmup)
@@ -265,6 +332,7 @@ def main():
         shoot_ms += b
     dprof.close()
 
+    log(f"profiled pass: setup {setup_ms:.2f} ms, shoot {shoot_ms:.2f} ms")
     # ---- exact walk counts over the same steps (deterministic solver)
     dcnt = capi.Device(scene, tree, opts, local)
     dcnt.set_counting(True)
@@ -274,6 +342,7 @@ def main():
     c1 = dcnt.stats()
     dcnt.close()
 
+    log("counting pass done")
     # ---- e2e: C ABI with host buffers (upload, K steps, download)
     barrier()
     te0 = time.perf_counter()
@@ -306,8 +375,14 @@ def main():
     h2d = dev_bytes / max(args.warmup + done, 1)
     d2h = n_slots * 16 * 4 / max(args.warmup + done, 1)
 
+    log(f"e2e {e2e_s:.3f} s")
+    batched = None
+    if args.batch_scenes > 0:
+        batched = measure_batched(capi, args.batch_scenes, args.warmup, args.batch_iters, local)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        log("cpu baseline")
         try:
             cpu = cpu_reference(tri, argv, 2, 60)
         except Exception as exc:
@@ -335,6 +410,7 @@ def main():
         "e2e": {"value": world * (args.warmup + done) / e2e_s, "unit": "shots/s",
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "note": "rad_dev_create (upload) + run + rad_dev_download over warm-up + timed steps"},
+        "batched": batched,
         "gpu_launches": 2 * done,
         "clocks": clocks.summary(),
         "cpu_baseline": cpu,

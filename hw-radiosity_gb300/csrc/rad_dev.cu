@@ -37,340 +37,10 @@
 
 #include "capi_internal.h"
 
+#include "rad_kernels.cuh"
+
 namespace radgb {
 namespace dev {
-
-constexpr int kShootThreads = 256;
-constexpr int kSlotsPerWarp = 10;
-constexpr int kSlotsPerCta = kSlotsPerWarp * (kShootThreads / 32);   // 80
-constexpr int kSetupThreads = 1024;
-constexpr int kMaxShooters = 256;
-constexpr double kPiD = 3.1415926535897932;
-constexpr unsigned kFull = 0xffffffffu;
-
-template <typename T> struct alignas(4 * sizeof(T)) Q4 { T x, y, z, w; };
-
-// integers carried in the 4th lane of a record, bit-exact
-__host__ __device__ inline float int_to_real(int v, float*) {
-#ifdef __CUDA_ARCH__
-    return __int_as_float(v);
-#else
-    float f; std::memcpy(&f, &v, 4); return f;
-#endif
-}
-__host__ __device__ inline double int_to_real(int v, double*) {
-    long long w = v;
-#ifdef __CUDA_ARCH__
-    return __longlong_as_double(w);
-#else
-    double d; std::memcpy(&d, &w, 8); return d;
-#endif
-}
-__device__ __forceinline__ int real_to_int(float f) { return __float_as_int(f); }
-__device__ __forceinline__ int real_to_int(double d) { return (int)__double_as_longlong(d); }
-template <typename T> inline T pack_int(int v) { return int_to_real(v, (T*)nullptr); }
-
-// order-preserving integer image of a key (+0 and -0 equal, as in the
-// reference's pair<float,int> comparison); candidates always map above 0
-__device__ __forceinline__ unsigned long long key_order(float f) {
-    unsigned u = __float_as_uint(f == 0.0f ? 0.0f : f);
-    return (u & 0x80000000u) ? (unsigned long long)(~u) : (unsigned long long)(u | 0x80000000u);
-}
-__device__ __forceinline__ unsigned long long key_order(double f) {
-    unsigned long long u = (unsigned long long)__double_as_longlong(f == 0.0 ? 0.0 : f);
-    return (u >> 63) ? ~u : (u | 0x8000000000000000ull);
-}
-
-// Visibility structure (kernel parameter; constant for a handle).
-template <typename T>
-struct Grid {
-    T g0[3], g1[3];
-    T inv_grid;                              // 1 / MinGridLen, for the first guess only
-    T t_eps, v_eps;                          // exact FP32 images of the 0.0001 and 1e-6 tests
-    int dims[3];
-    int thr_off[3];
-    int n_thr;
-    const T* thr;                            // cell-coordinate thresholds (global; staged to smem)
-    const int32_t* __restrict__ cell_leaf;   // cell coordinate triple -> leaf
-    const Q4<T>* __restrict__ leaf;          // 2 per leaf: (g0, begin) (g1, end)
-    const Q4<T>* __restrict__ entry;         // 5 per list entry: (n, id) (c, 0) se0 se1 se2
-    int walk_cap;
-};
-
-// Slot store, SoA of 4-wide records.
-template <typename T>
-struct Slots {
-    int n;
-    const Q4<T>* __restrict__ vtx;   // 3 per slot
-    const Q4<T>* __restrict__ nrm;   // normal, w = |n| (norm() of the reference)
-    const Q4<T>* __restrict__ ctr;   // centre, w = area
-    const Q4<T>* __restrict__ frgb;  // reflectance 0..255, w = parent
-    Q4<T>* accB;                     // 3 per slot (w unused)
-    Q4<T>* deltaB;                   // 1 per slot (w unused)
-};
-
-template <typename T>
-struct Patch { T c[3]; T area; };
-
-template <typename T>
-struct Shooter {
-    int slot, logsrc, split, pad;
-    T n[3];
-    T nlen;
-    T deltaB[3];
-    T pad2;
-    Patch<T> part[3];   // whole source, half 1, half 2
-};
-
-struct Partial { unsigned long long key; int slot; int pad; };
-
-// dynamic shared memory of k_shoot: shooter records, then the thresholds
-template <typename T>
-__host__ __device__ inline size_t kMaxShooterBytes(int nsh) {
-    return ((size_t)nsh * sizeof(Shooter<T>) + 15) & ~(size_t)15;
-}
-
-struct State {
-    int work;               // next 10-slot group of the current step (k_shoot queue)
-    int done;               // a selection found no candidate
-    int paused;             // step limit reached
-    int nsh;                // shooters of the current step
-    int err;
-    long long steps;
-    long long step_limit;
-    long long trace_cap;
-    int* trace;
-    unsigned long long rays, rays_ref, cells, tris, se, prec, capped;
-};
-
-struct Cnt { unsigned rays, rays_ref, cells, tris, se, prec, capped; };
-
-// Cell coordinate along one axis: a first guess in T, corrected against the
-// thresholds so the result equals the reference's FP64 expression exactly.
-template <typename T>
-__device__ __forceinline__ int cell_axis(T q, T g0, T inv, const T* th, int D) {
-    int k = (int)((q - g0) * inv);
-    k = min(max(k, 0), D - 1);
-    while (k + 1 < D && q >= th[k + 1]) ++k;
-    while (k > 0 && q < th[k]) --k;
-    return k;
-}
-
-// ------------------------------------------------------------------ walk
-// RayHitted (raycast.cpp:335-360) with TreeNodeNum (254-281) as a table
-// lookup, TriListHitted/TriHitted (283-333) and NextPoint (235-251).
-template <typename T, bool COUNT>
-__device__ __forceinline__ int walk(const Grid<T>& G, const T p[3], const T v[3], int ban, Cnt& c) {
-    T t = 0;
-    int prev = -1;
-    T q0 = p[0], q1 = p[1], q2 = p[2];
-    for (int it = 0; it < G.walk_cap; ++it) {
-        if (q0 < G.g0[0] || q0 > G.g1[0] || q1 < G.g0[1] || q1 > G.g1[1] || q2 < G.g0[2] || q2 > G.g1[2])
-            return -1;
-        if (COUNT) c.cells++;
-        // (int)(((double)q - G0) / MinGridLen) per axis, found exactly from the thresholds
-        const int gx = cell_axis(q0, G.g0[0], G.inv_grid, G.thr + G.thr_off[0], G.dims[0]);
-        const int gy = cell_axis(q1, G.g0[1], G.inv_grid, G.thr + G.thr_off[1], G.dims[1]);
-        const int gz = cell_axis(q2, G.g0[2], G.inv_grid, G.thr + G.thr_off[2], G.dims[2]);
-        const int leaf = __ldg(&G.cell_leaf[(gx * G.dims[1] + gy) * G.dims[2] + gz]);
-        if (leaf == prev) {          // "Precision Exceeded": step one unit of t
-            if (COUNT) c.prec++;
-            t = (T)((double)t + 1.0);
-            q0 = p[0] + t * v[0]; q1 = p[1] + t * v[1]; q2 = p[2] + t * v[2];
-            continue;
-        }
-        const Q4<T> lo = G.leaf[2 * leaf], hi = G.leaf[2 * leaf + 1];
-        const int b = real_to_int(lo.w), e = real_to_int(hi.w);
-        T tmin = (T)1000000.0;
-        int best = -1;
-        for (int k = b; k < e; ++k) {
-            const Q4<T> en = G.entry[5 * k];
-            const int id = real_to_int(en.w);
-            if (id == ban) continue;
-            const Q4<T> ec = G.entry[5 * k + 1];
-            if (COUNT) c.tris++;
-            const T a1 = v[0] * en.x + v[1] * en.y + v[2] * en.z;
-            const T w0 = ec.x - p[0], w1 = ec.y - p[1], w2 = ec.z - p[2];
-            const T a2 = w0 * en.x + w1 * en.y + w2 * en.z;
-            const T tt = a2 / a1;
-            if (tt < G.t_eps) continue;            // (double)t < 0.0001
-            if (tt >= tmin) continue;
-            if (COUNT) c.se++;
-            const T x = p[0] + tt * v[0], y = p[1] + tt * v[1], z = p[2] + tt * v[2];
-            const Q4<T> s0 = G.entry[5 * k + 2];
-            if ((x * s0.x + y * s0.y + z * s0.z + s0.w) < 0.0) continue;
-            const Q4<T> s1 = G.entry[5 * k + 3];
-            if ((x * s1.x + y * s1.y + z * s1.z + s1.w) < 0.0) continue;
-            const Q4<T> s2 = G.entry[5 * k + 4];
-            if ((x * s2.x + y * s2.y + z * s2.z + s2.w) < 0.0) continue;
-            tmin = tt;
-            best = id;
-        }
-        if (best >= 0) return best;
-        prev = leaf;
-        // NextPoint: leave the cell from the ray origin, overshoot by 0.1 in t
-        const T bl[3] = {lo.x, lo.y, lo.z}, bh[3] = {hi.x, hi.y, hi.z};
-        T tm = (T)1000000.0;
-#pragma unroll
-        for (int a = 0; a < 3; a++) {
-            if (fabs(v[a]) > G.v_eps) {             // fabs((double)v) > 1e-6
-                const T s = (v[a] > 0) ? (bh[a] - p[a]) / v[a] : (bl[a] - p[a]) / v[a];
-                tm = (s < tm) ? s : tm;
-            }
-        }
-        tm = (T)((double)tm + 0.1);
-        q0 = p[0] + tm * v[0]; q1 = p[1] + tm * v[1]; q2 = p[2] + tm * v[2];
-        t = tm;
-    }
-    c.capped++;
-    return -2;
-}
-
-template <typename T> __device__ __forceinline__ T rsqrt_exact(T x);
-template <> __device__ __forceinline__ float rsqrt_exact<float>(float x) { return sqrtf(x); }
-template <> __device__ __forceinline__ double rsqrt_exact<double>(double x) { return sqrt(x); }
-
-// CalFF, shade.cpp:107-127: the pre-test is cheap, the walk is not
-template <typename T, bool COUNT, bool WALK>
-__device__ __forceinline__ T point_ff(const Shooter<T>& s, const Patch<T>& src, const T p[3], const T nd[3], T ndlen,
-                                      int logdes, const Grid<T>& G, Cnt& c) {
-    const T d[3] = {src.c[0] - p[0], src.c[1] - p[1], src.c[2] - p[2]};
-    const T ds = d[0] * s.n[0] + d[1] * s.n[1] + d[2] * s.n[2];
-    const T dd = -(d[0] * nd[0] + d[1] * nd[1] + d[2] * nd[2]);
-    if ((ds < 0) != (dd < 0)) return 0;
-    const T d2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
-    const T dl = rsqrt_exact<T>(d2);
-    const T c1 = ds / dl / s.nlen;
-    const T c2 = dd / dl / ndlen;
-    T ff = c1 * c2;
-    if (ff <= 0.0) return 0;
-    ff = (T)((double)ff * ((double)src.area / ((double)d2 * kPiD)));
-    if (ff <= 0.0) return 0;
-    if (!WALK) return ff;   // pre-test only (reference ray accounting)
-    c.rays++;
-    return walk<T, COUNT>(G, p, d, logdes, c) == s.logsrc ? ff : (T)0;
-}
-
-// Shade's per-corner AdaptCalFF(CalFF(...)), shade.cpp:442-450 with the
-// stray ';' at shade.cpp:164: a split source returns ff(half1)+ff(half2); the
-// whole-source result is discarded, so its walk is not cast.
-template <typename T, bool COUNT>
-__device__ __forceinline__ T corner_ff(const Shooter<T>& s, const T p[3], const T nd[3], T ndlen, int logdes,
-                                       const Grid<T>& G, Cnt& c) {
-    const unsigned before = c.rays;
-    if (!s.split) {
-        const T f = point_ff<T, COUNT, true>(s, s.part[0], p, nd, ndlen, logdes, G, c);
-        if (COUNT) c.rays_ref += c.rays - before;
-        return f;
-    }
-    if (COUNT && point_ff<T, COUNT, false>(s, s.part[0], p, nd, ndlen, logdes, G, c) > (T)0) c.rays_ref++;
-    const T f1 = point_ff<T, COUNT, true>(s, s.part[1], p, nd, ndlen, logdes, G, c);
-    const T f2 = point_ff<T, COUNT, true>(s, s.part[2], p, nd, ndlen, logdes, G, c);
-    if (COUNT) c.rays_ref += c.rays - before;
-    return f1 + f2;
-}
-
-template <typename T>
-__device__ __forceinline__ T shfl(T v, int src) { return __shfl_sync(kFull, v, src); }
-
-__device__ __forceinline__ bool part_less(unsigned long long ka, int ia, unsigned long long kb, int ib) {
-    return ka < kb || (ka == kb && ia < ib);
-}
-
-__device__ __forceinline__ void warp_max(unsigned long long& k, int& i) {
-#pragma unroll
-    for (int o = 16; o; o >>= 1) {
-        unsigned long long k2 = __shfl_xor_sync(kFull, k, o);
-        int i2 = __shfl_xor_sync(kFull, i, o);
-        if (part_less(k, i, k2, i2)) { k = k2; i = i2; }
-    }
-}
-
-template <bool COUNT>
-__device__ __forceinline__ void flush_counters(State* st, Cnt& c, int lane) {
-    unsigned v[7] = {c.rays, c.rays_ref, c.cells, c.tris, c.se, c.prec, c.capped};
-    unsigned long long* dst[7] = {&st->rays, &st->rays_ref, &st->cells, &st->tris, &st->se, &st->prec, &st->capped};
-    const int nc = COUNT ? 7 : 1;
-#pragma unroll
-    for (int q = 0; q < 7; q++) {
-        if (q >= nc && q != 6) continue;
-        unsigned s = __reduce_add_sync(kFull, v[q]);
-        if (lane == 0 && s) atomicAdd(dst[q], (unsigned long long)s);
-    }
-}
-
-// ------------------------------------------------------------------ k_shoot
-// One 10-slot group: lanes 3r+v are corner v of slot g*10+r.
-template <typename T, bool COUNT>
-__device__ __forceinline__ void shoot_group(const Slots<T>& S, const Grid<T>& G, const Shooter<T>* sh, int nsh,
-                                            int g, int lane, T conv, unsigned long long& kk, int& ks, Cnt& c) {
-    const int r = lane / 3, v = lane - 3 * r;
-    const int i = g * kSlotsPerWarp + r;
-    const bool own = lane < 3 * kSlotsPerWarp && i < S.n;
-
-    Q4<T> fr = {0, 0, 0, (T)-1}, acc = {0, 0, 0, 0}, db = {0, 0, 0, 0};
-    if (own) {
-        fr = S.frgb[i];
-        acc = S.accB[i * 3 + v];
-    }
-    const int parent = (int)fr.w;
-    const bool live = own && parent >= 0;
-    bool is_src = false;
-    for (int j = 0; j < nsh; j++) is_src |= (sh[j].slot == i);
-    // a receiver is skipped only when all nine accB components are >= 255
-    const bool open_v = live && (acc.x < (T)255 || acc.y < (T)255 || acc.z < (T)255);
-    const unsigned ballot = __ballot_sync(kFull, open_v);
-    const int base = 3 * min(r, kSlotsPerWarp - 1);
-    const bool open = ((ballot >> base) & 7u) != 0;
-    const bool active = live && !is_src && open && nsh > 0;
-    if (live && v == 0) db = S.deltaB[i];
-
-    T pv[3] = {0, 0, 0}, nd[3] = {0, 0, 0}, ndlen = 1;
-    if (active) {
-        const Q4<T> pp = S.vtx[i * 3 + v];
-        const Q4<T> nn = S.nrm[i];
-        pv[0] = pp.x; pv[1] = pp.y; pv[2] = pp.z;
-        nd[0] = nn.x; nd[1] = nn.y; nd[2] = nn.z;
-        ndlen = nn.w;
-    }
-    const T k = (T)(0.5 / 255.0);   // RefRatio / 255.0, shade.cpp:246
-    T a0 = acc.x, a1 = acc.y, a2 = acc.z;
-    T d0 = db.x, d1 = db.y, d2 = db.z;
-    for (int j = 0; j < nsh; j++) {
-        T ff = 0;
-        if (active) ff = corner_ff<T, COUNT>(sh[j], pv, nd, ndlen, parent, G, c);
-        const T f0 = shfl(ff, base), f1 = shfl(ff, base + 1), f2 = shfl(ff, base + 2);
-        if (active) {
-            const T lo0 = fr.x * k * sh[j].deltaB[0] / 3;
-            const T lo1 = fr.y * k * sh[j].deltaB[1] / 3;
-            const T lo2 = fr.z * k * sh[j].deltaB[2] / 3;
-            a0 += lo0 * ff; a1 += lo1 * ff; a2 += lo2 * ff;
-            if (v == 0) {
-                d0 += lo0 * f0; d0 += lo0 * f1; d0 += lo0 * f2;
-                d1 += lo1 * f0; d1 += lo1 * f1; d1 += lo1 * f2;
-                d2 += lo2 * f0; d2 += lo2 * f1; d2 += lo2 * f2;
-            }
-        }
-    }
-    if (active) {
-        Q4<T> o = {a0, a1, a2, acc.w};
-        S.accB[i * 3 + v] = o;
-        if (v == 0) { Q4<T> q = {d0, d1, d2, db.w}; S.deltaB[i] = q; }
-    }
-    if (live && is_src && v == 0) {       // rad.cpp:446-449
-        d0 = d1 = d2 = 0;
-        Q4<T> q = {0, 0, 0, db.w};
-        S.deltaB[i] = q;
-    }
-    // next selection: key = (dB0 + dB1) + dB2 (rad.cpp:394), candidates > converge
-    if (live && v == 0) {
-        const T key = (d0 + d1) + d2;
-        if (key > conv) {
-            const unsigned long long o = key_order(key);
-            if (part_less(kk, ks, o, i)) { kk = o; ks = i; }
-        }
-    }
-}
 
 // Persistent: each warp takes 10-slot groups from the step's queue until it
 // is empty, so warps that finish early take more work; the CTA's (key, slot)
@@ -429,49 +99,6 @@ k_shoot(Slots<T> S, Grid<T> G, const Shooter<T>* __restrict__ shooters, State* s
 }
 
 // ------------------------------------------------------------------ k_setup
-template <typename T>
-__device__ void build_shooter(const Slots<T>& S, int slot, Shooter<T>& s) {
-    const Q4<T> fr = S.frgb[slot], nn = S.nrm[slot], cc = S.ctr[slot], db = S.deltaB[slot];
-    T p[3][3];
-    for (int v = 0; v < 3; v++) {
-        const Q4<T> q = S.vtx[slot * 3 + v];
-        p[v][0] = q.x; p[v][1] = q.y; p[v][2] = q.z;
-    }
-    s.slot = slot;
-    s.logsrc = (int)fr.w;
-    s.pad = 0;
-    s.n[0] = nn.x; s.n[1] = nn.y; s.n[2] = nn.z;
-    s.nlen = nn.w;
-    s.deltaB[0] = db.x; s.deltaB[1] = db.y; s.deltaB[2] = db.z;
-    s.pad2 = 0;
-    s.part[0].c[0] = cc.x; s.part[0].c[1] = cc.y; s.part[0].c[2] = cc.z;
-    s.part[0].area = cc.w;
-    // AdaptCalFF's split decision (shade.cpp:143-156): first longest edge
-    int e = 0;
-    T longest = 0;
-    for (int v = 0; v < 3; v++) {
-        const T l0 = p[(v + 1) % 3][0] - p[v][0], l1 = p[(v + 1) % 3][1] - p[v][1], l2 = p[(v + 1) % 3][2] - p[v][2];
-        const T len = l0 * l0 + l1 * l1 + l2 * l2;
-        if (longest < len) { longest = len; e = v; }
-    }
-    s.split = !((double)longest < 0.1);
-    if (s.split) {   // PartitionSource, shade.cpp:76-99
-        const int i0 = e, i1 = (e + 1) % 3, i2 = (e + 2) % 3;
-        T m[3];
-        for (int q = 0; q < 3; q++) m[q] = (T)((double)(p[i0][q] + p[i1][q]) / 2.0);
-        for (int q = 0; q < 3; q++) {
-            s.part[1].c[q] = (T)((double)(m[q] + p[i2][q] + p[i0][q]) / 3.0);
-            s.part[2].c[q] = (T)((double)(m[q] + p[i1][q] + p[i2][q]) / 3.0);
-        }
-        s.part[1].area = s.part[2].area = (T)((double)cc.w / 2.0);
-    } else {
-        for (int h = 1; h < 3; h++) {
-            for (int q = 0; q < 3; q++) s.part[h].c[q] = 0;
-            s.part[h].area = 0;
-        }
-    }
-}
-
 template <typename T>
 __global__ void __launch_bounds__(kSetupThreads)
 k_setup(Slots<T> S, Shooter<T>* shooters, State* st, const Partial* __restrict__ part, int nparts, T conv, int P) {
@@ -709,74 +336,30 @@ int upload(const Scene<T>& s, const Octree<T>& o, const rad_options& opt, int de
     d.conv = (T)opt.converge;
     const int n = s.trinum;
     if (n < 0) return fail(RAD_ERR_ARG, "negative slot count");
-    // slot records
-    std::vector<Q4<T>> vtx((size_t)n * 3), nrm(n), ctr(n), frgb(n), acc((size_t)n * 3), db(n);
-    for (int i = 0; i < n; i++) {
-        const Slot<T>& t = s.slots[i];
-        for (int v = 0; v < 3; v++) {
-            vtx[i * 3 + v] = {t.p[v][0], t.p[v][1], t.p[v][2], 0};
-            acc[i * 3 + v] = {t.accB[v][0], t.accB[v][1], t.accB[v][2], 0};
-        }
-        const T nl = (T)std::sqrt(t.n[0] * t.n[0] + t.n[1] * t.n[1] + t.n[2] * t.n[2]);
-        nrm[i] = {t.n[0], t.n[1], t.n[2], nl};
-        ctr[i] = {t.c[0], t.c[1], t.c[2], t.area};
-        frgb[i] = {(T)t.Frgb[0], (T)t.Frgb[1], (T)t.Frgb[2], (T)t.parent};
-        db[i] = {t.deltaB[0], t.deltaB[1], t.deltaB[2], 0};
-    }
-    Q4<T> *d_vtx, *d_nrm, *d_ctr, *d_frgb, *d_acc, *d_db;
-    int rc;
-    if ((rc = d.alloc(&d_vtx, vtx.size())) || (rc = d.alloc(&d_nrm, nrm.size())) || (rc = d.alloc(&d_ctr, ctr.size())) ||
-        (rc = d.alloc(&d_frgb, frgb.size())) || (rc = d.alloc(&d_acc, acc.size())) || (rc = d.alloc(&d_db, db.size())))
-        return rc;
-    CU(cudaMemcpyAsync(d_vtx, vtx.data(), vtx.size() * sizeof(Q4<T>), cudaMemcpyHostToDevice, d.stream));
-    CU(cudaMemcpyAsync(d_nrm, nrm.data(), nrm.size() * sizeof(Q4<T>), cudaMemcpyHostToDevice, d.stream));
-    CU(cudaMemcpyAsync(d_ctr, ctr.data(), ctr.size() * sizeof(Q4<T>), cudaMemcpyHostToDevice, d.stream));
-    CU(cudaMemcpyAsync(d_frgb, frgb.data(), frgb.size() * sizeof(Q4<T>), cudaMemcpyHostToDevice, d.stream));
-    CU(cudaMemcpyAsync(d_acc, acc.data(), acc.size() * sizeof(Q4<T>), cudaMemcpyHostToDevice, d.stream));
-    CU(cudaMemcpyAsync(d_db, db.data(), db.size() * sizeof(Q4<T>), cudaMemcpyHostToDevice, d.stream));
-    d.S = Slots<T>{n, d_vtx, d_nrm, d_ctr, d_frgb, d_acc, d_db};
-
     if (!thresholds_consistent(o)) return fail(RAD_ERR_ARG, "octree cell thresholds do not match its dimensions");
-    // visibility structure; the walk's triangle records come from the current slots
-    const int n_leaves = (int)(o.leaf_range.size() / 2);
-    const size_t n_ent = o.entry_tri.size();
-    std::vector<Q4<T>> leaf((size_t)n_leaves * 2), ent(n_ent * 5);
-    for (int l = 0; l < n_leaves; l++) {
-        const T* b = &o.leaf_box[(size_t)l * 8];
-        leaf[2 * l] = {b[0], b[1], b[2], pack_int<T>(o.leaf_range[2 * l])};
-        leaf[2 * l + 1] = {b[4], b[5], b[6], pack_int<T>(o.leaf_range[2 * l + 1])};
-    }
-    for (size_t k = 0; k < n_ent; k++) {
-        const int id = o.entry_tri[k];
-        const Slot<T>& t = s.slots[id];
-        ent[5 * k] = {t.n[0], t.n[1], t.n[2], pack_int<T>(id)};
-        ent[5 * k + 1] = {t.c[0], t.c[1], t.c[2], 0};
-        for (int e = 0; e < 3; e++) ent[5 * k + 2 + e] = {t.se[e][0], t.se[e][1], t.se[e][2], t.se[e][3]};
-    }
-    Q4<T> *d_leaf, *d_ent;
-    int32_t* d_cell;
-    if ((rc = d.alloc(&d_leaf, leaf.size())) || (rc = d.alloc(&d_ent, ent.size())) ||
-        (rc = d.alloc(&d_cell, o.cell_leaf.size())))
-        return rc;
-    CU(cudaMemcpyAsync(d_leaf, leaf.data(), leaf.size() * sizeof(Q4<T>), cudaMemcpyHostToDevice, d.stream));
-    CU(cudaMemcpyAsync(d_ent, ent.data(), ent.size() * sizeof(Q4<T>), cudaMemcpyHostToDevice, d.stream));
-    CU(cudaMemcpyAsync(d_cell, o.cell_leaf.data(), o.cell_leaf.size() * 4, cudaMemcpyHostToDevice, d.stream));
+    HostPack<T> P;
+    pack_scene(s, o, P);
+    Q4<T> *d_vtx, *d_nrm, *d_ctr, *d_frgb, *d_acc, *d_db, *d_leaf, *d_ent;
+    int4* d_cell;
     T* d_thr;
-    if ((rc = d.alloc(&d_thr, o.thr.size()))) return rc;
-    CU(cudaMemcpyAsync(d_thr, o.thr.data(), o.thr.size() * sizeof(T), cudaMemcpyHostToDevice, d.stream));
-    Grid<T> G{};
-    for (int k = 0; k < 3; k++) {
-        G.g0[k] = o.G0[k]; G.g1[k] = o.G1[k]; G.dims[k] = o.dims[k]; G.thr_off[k] = o.thr_off[k];
-    }
-    G.inv_grid = (T)(1.0 / (double)o.min_grid);
-    G.t_eps = o.t_eps;
-    G.v_eps = o.v_eps;
-    G.n_thr = (int)o.thr.size();
+    int rc;
+    auto put = [&](auto** dst, const auto& src) -> int {
+        int r = d.alloc(dst, src.size());
+        if (r) return r;
+        CU(cudaMemcpyAsync(*dst, src.data(), src.size() * sizeof(src[0]), cudaMemcpyHostToDevice, d.stream));
+        return RAD_OK;
+    };
+    if ((rc = put(&d_vtx, P.vtx)) || (rc = put(&d_nrm, P.nrm)) || (rc = put(&d_ctr, P.ctr)) ||
+        (rc = put(&d_frgb, P.frgb)) || (rc = put(&d_acc, P.acc)) || (rc = put(&d_db, P.db)) ||
+        (rc = put(&d_leaf, P.leaf)) || (rc = put(&d_ent, P.ent)) || (rc = put(&d_cell, P.cell)) ||
+        (rc = put(&d_thr, P.thr)))
+        return rc;
+    d.S = Slots<T>{n, d_vtx, d_nrm, d_ctr, d_frgb, d_acc, d_db};
+    Grid<T> G = grid_params(o, opt.walk_cap);
     G.thr = d_thr;
-    G.cell_leaf = d_cell;
+    G.cell = d_cell;
     G.leaf = d_leaf;
     G.entry = d_ent;
-    G.walk_cap = opt.walk_cap > 0 ? opt.walk_cap : (1 << 20);
     d.G = G;
 
     // per-step state; k_shoot is persistent: as many CTAs as fit at once

@@ -31,7 +31,7 @@ NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "--prec-di
                      "-Xcompiler", "-fPIC,-ffp-contract=off", f"-I{INC}", "-Xptxas", "-v"]
 
 HOST_SRC = ["scene.cpp", "octree.cpp", "capi.cpp"]
-CUDA_SRC = ["rad_dev.cu"]
+CUDA_SRC = ["rad_dev.cu", "rad_batch.cu"]
 
 
 def _nvcc() -> str:
@@ -60,7 +60,8 @@ def build(verbose: bool = False, force: bool = False) -> dict:
     os.makedirs(OBJ, exist_ok=True)
     os.makedirs(os.path.dirname(LIB), exist_ok=True)
     os.makedirs(os.path.dirname(BIN), exist_ok=True)
-    headers = [os.path.join(CSRC, h) for h in os.listdir(CSRC) if h.endswith(".h")] + [os.path.join(INC, "rad_gb300.h")]
+    headers = [os.path.join(CSRC, h) for h in os.listdir(CSRC) if h.endswith((".h", ".cuh"))] + \
+        [os.path.join(INC, "rad_gb300.h")]
     nvcc = _nvcc()
     log: list = []
     jobs = []

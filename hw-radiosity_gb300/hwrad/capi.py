@@ -27,6 +27,8 @@ EXPORTS = [
     "rad_dev_create", "rad_dev_run", "rad_dev_run_timed", "rad_dev_run_profiled", "rad_dev_download", "rad_dev_trace", "rad_dev_stats",
     "rad_dev_set_counting", "rad_dev_ray_hit", "rad_dev_form_factors", "rad_dev_form_factors_noalloc",
     "rad_dev_destroy",
+    "rad_batch_create", "rad_batch_run", "rad_batch_run_timed", "rad_batch_scene_stats", "rad_batch_download",
+    "rad_batch_trace", "rad_batch_stats", "rad_batch_set_counting", "rad_batch_destroy",
 ]
 
 
@@ -105,6 +107,15 @@ def load(path: Optional[str] = None) -> C.CDLL:
         "rad_dev_form_factors": (C.c_int, [vp, i32, vp, i32, vp]),
         "rad_dev_form_factors_noalloc": (C.c_int, [vp, vp, i32, vp, i32, vp, vp]),
         "rad_dev_destroy": (None, [vp]),
+        "rad_batch_create": (C.c_int, [vp, vp, vp, i32, i32, i32, P(vp)]),
+        "rad_batch_run": (C.c_int, [vp, i64, P(i64), P(i32)]),
+        "rad_batch_run_timed": (C.c_int, [vp, i64, P(i64), P(i32), P(C.c_double)]),
+        "rad_batch_scene_stats": (C.c_int, [vp, i32, P(i64), P(i32)]),
+        "rad_batch_download": (C.c_int, [vp, i32, vp]),
+        "rad_batch_trace": (C.c_int, [vp, i32, vp, i64, P(i64)]),
+        "rad_batch_stats": (C.c_int, [vp, P(Stats)]),
+        "rad_batch_set_counting": (C.c_int, [vp, i32]),
+        "rad_batch_destroy": (None, [vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -324,6 +335,68 @@ class Device:
     def close(self):
         if self.h:
             load().rad_dev_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Batch:
+    """Batched form (``rad_batch``): independent scenes, one launch per iteration."""
+
+    def __init__(self, scenes, trees, opts, device: int = 0, trace_cap: int = 0):
+        n = len(scenes)
+        self._keep = (list(scenes), list(trees), list(opts))
+        sp = (C.c_void_p * n)(*[s.h.value for s in scenes])
+        tp = (C.c_void_p * n)(*[t.h.value for t in trees])
+        op = (Options * n)(*opts)
+        self._opts = op
+        self.n = n
+        self.h = C.c_void_p()
+        _check(load().rad_batch_create(C.cast(sp, C.c_void_p), C.cast(tp, C.c_void_p), C.cast(op, C.c_void_p),
+                                       n, trace_cap, device, C.byref(self.h)))
+
+    def run(self, max_iters: int = 1 << 62):
+        it, na = C.c_int64(), C.c_int32()
+        rc = _check(load().rad_batch_run(self.h, max_iters, C.byref(it), C.byref(na)), allow=(RAD_ERR_WALK,))
+        return it.value, na.value, rc
+
+    def run_timed(self, max_iters: int):
+        it, na, ms = C.c_int64(), C.c_int32(), C.c_double()
+        _check(load().rad_batch_run_timed(self.h, max_iters, C.byref(it), C.byref(na), C.byref(ms)),
+               allow=(RAD_ERR_WALK,))
+        return it.value, na.value, ms.value
+
+    def scene_stats(self, s: int):
+        st, cv = C.c_int64(), C.c_int32()
+        _check(load().rad_batch_scene_stats(self.h, s, C.byref(st), C.byref(cv)))
+        return st.value, bool(cv.value)
+
+    def download(self, s: int, scene: "Scene"):
+        _check(load().rad_batch_download(self.h, s, scene.h))
+
+    def trace(self, s: int) -> np.ndarray:
+        n = C.c_int64()
+        _check(load().rad_batch_trace(self.h, s, None, 0, C.byref(n)))
+        out = np.zeros(n.value, np.int32)
+        if n.value:
+            _check(load().rad_batch_trace(self.h, s, out.ctypes.data, n.value, C.byref(n)))
+        return out.reshape(-1, 1)
+
+    def stats(self) -> Dict[str, int]:
+        s = Stats()
+        _check(load().rad_batch_stats(self.h, C.byref(s)))
+        return {k: getattr(s, k) for k, _ in Stats._fields_}
+
+    def set_counting(self, on: bool):
+        _check(load().rad_batch_set_counting(self.h, 1 if on else 0))
+
+    def close(self):
+        if self.h:
+            load().rad_batch_destroy(self.h)
             self.h = C.c_void_p()
 
     def __del__(self):

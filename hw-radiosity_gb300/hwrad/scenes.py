@@ -287,6 +287,53 @@ def hall(target_tris: int = 400_000, n_pillars: int = 300, seed: int = 3000,
                  np.concatenate(br).astype(np.int32), opts, name or "config3_hall")
 
 
+def _rotation(axis, angle):
+    a = np.asarray(axis, np.float64)
+    a = a / np.linalg.norm(a)
+    c, s_ = math.cos(angle), math.sin(angle)
+    x, y, z = a
+    return np.array([[c + x * x * (1 - c), x * y * (1 - c) - z * s_, x * z * (1 - c) + y * s_],
+                     [y * x * (1 - c) + z * s_, c + y * y * (1 - c), y * z * (1 - c) - x * s_],
+                     [z * x * (1 - c) - y * s_, z * y * (1 - c) + x * s_, c + z * z * (1 - c)]])
+
+
+def precision_stress(n_slabs: int = 64, seed: int = 5000, thickness: float = 1e-3) -> Scene:
+    """The 768-triangle room with emitters spanning a 1e4 power range and thin
+    slabs at grazing angles to them (the precision stress case).
+
+    Emitters: the centre 2x2 ceiling quads.  A light needs one background
+    channel equal to 255 and every light shares the global -light scale, so
+    the range is carried by the other channels: one quad is (255, X, X) with
+    X chosen so its total emission is 1e4 times that of the three (255, 0, 0)
+    quads; with -light = 0.1/255 those emit (0.1, 0, 0) and the strong one
+    about (0.1, 500, 500).
+    Slabs: 1.5 x thickness x 1.5 boxes, tilted 1-5 degrees off vertical
+    (nearly parallel to the downward emitter rays), seeded positions."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    scale = 0.1 / 255.0
+    X = int(round((1e4 * 255 - 255) / 2))
+    base = room(8, light_scale=scale)
+    vtx, fr, br = base.vtx.copy(), base.frgb.copy(), base.brgb.copy()
+    lights = np.nonzero((br == 255).any(axis=1))[0]
+    # the first light quad (two triangles) becomes the strong emitter
+    br[lights] = (255, 0, 0)
+    br[lights[:2]] = (255, X, X)
+    parts = [Scene(vtx, fr, br, {})]
+    for _ in range(n_slabs):
+        lo = np.array([-0.75, -thickness / 2, -0.75])
+        hi = -lo
+        t, f, b = _box_tris(lo, hi, 1, np.rint(255 * rng.uniform(0.2, 0.8, 3)).astype(np.int32))
+        # stand the slab up (its thin axis horizontal), then tilt it slightly
+        R = _rotation((1, 0, 0), math.pi / 2) @ _rotation(rng.normal(size=3), math.radians(rng.uniform(1, 5)))
+        R = _rotation((0, 1, 0), rng.uniform(0, 2 * math.pi)) @ R
+        c = rng.uniform((1.5, 1.0, 1.5), (8.5, 8.0, 8.5))
+        t = t @ R.T + c
+        parts.append(Scene(t.astype(np.float32), f, b, {}))
+    key = 100.0 * (255 + 2 * X) * scale
+    opts = {"-light": repr(float(np.float32(scale))), "-converge": repr(float(np.float32(1e-3 * key)))}
+    return concat(parts, opts, "config5_precision")
+
+
 def batch_rooms(n_scenes: int = 256, seed: int = 4000, lo: int = 500, hi: int = 50_000,
                 max_boxes: int = 32) -> List[Scene]:
     """Independent rooms with per-scene seeds; triangle counts log-uniform in

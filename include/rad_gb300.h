@@ -56,6 +56,7 @@ typedef struct rad_options {
 typedef struct rad_scene rad_scene;   /* host scene store */
 typedef struct rad_octree rad_octree; /* host-built visibility structure */
 typedef struct rad_dev rad_dev;       /* device-resident solver */
+typedef struct rad_batch rad_batch;   /* many independent scenes shot together */
 
 /* Read-only view of a scene's live slots (valid until the scene changes or
  * is freed).  Arrays are slot-major; element type float (precision 32) or
@@ -199,6 +200,32 @@ int rad_dev_form_factors(rad_dev* d, int32_t src, const int32_t* rcv, int32_t n,
 int rad_dev_form_factors_noalloc(rad_dev* d, const int32_t* src, int32_t n_src, const int32_t* d_rcv, int32_t n_rcv,
                                  void* d_ff, void* stream);
 void rad_dev_destroy(rad_dev* d);
+
+/* ---- batched form -------------------------------------------------------- */
+
+/* Upload n_scenes independent scenes (each after init + pre-partition, with
+ * its own options: converge limit, walk cap) for the batched form: every
+ * iteration, each scene that has not converged does one shooter step of
+ * parallelRadiosity (src/rad.cpp:406-451) with one shooter, all scenes in one
+ * persistent launch.  FP32 only; parallel_src must be 1.  Each scene's result
+ * is bit-identical to rad_dev_run on that scene.  trace_cap: shooter ids kept
+ * per scene (default 65536 when <= 0). */
+int rad_batch_create(const rad_scene* const* scenes, const rad_octree* const* trees, const rad_options* opts,
+                     int32_t n_scenes, int32_t trace_cap, int32_t device, rad_batch** out);
+/* Run up to max_iters batch iterations; stops when every scene converged.
+ * *iters_done: iterations in which at least one scene was running (a scene's
+ * last iteration is the one whose selection finds no candidate);
+ * *n_active: scenes still running. */
+int rad_batch_run(rad_batch* b, int64_t max_iters, int64_t* iters_done, int32_t* n_active);
+/* As rad_batch_run, also reporting the device time of the iterations (ms). */
+int rad_batch_run_timed(rad_batch* b, int64_t max_iters, int64_t* iters_done, int32_t* n_active, double* device_ms);
+int rad_batch_scene_stats(const rad_batch* b, int32_t scene, int64_t* steps, int32_t* converged);
+int rad_batch_download(rad_batch* b, int32_t scene, rad_scene* s);
+int rad_batch_trace(const rad_batch* b, int32_t scene, int32_t* out, int64_t cap, int64_t* n);
+/* Totals over all scenes (steps = shooter steps of all scenes). */
+int rad_batch_stats(const rad_batch* b, rad_stats* st);
+int rad_batch_set_counting(rad_batch* b, int32_t on);
+void rad_batch_destroy(rad_batch* b);
 
 #ifdef __cplusplus
 }

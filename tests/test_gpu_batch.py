@@ -1,0 +1,87 @@
+"""Batched form: every scene's result equals the single-scene solver's, bit for bit."""
+import os
+
+import numpy as np
+import pytest
+
+import runner
+from helpers import same_bits
+from hwrad import capi, scenes
+
+pytestmark = pytest.mark.gpu
+
+
+def _prep(sc, workdir, name, extra=None):
+    tri = sc.write(os.path.join(workdir, f"{name}.tri"))
+    argv = sc.argv(extra)
+    o = capi.options_from_argv(argv)
+    s = capi.Scene.load(tri, o)
+    t = capi.Octree(s, 2)
+    s.init()
+    s.prepartition()
+    return tri, argv, o, s, t
+
+
+def _scenes():
+    out = [scenes.room(4, emitter=(0.25, 0.75)), scenes.room(8), scenes.room(8, size=100.0),
+           scenes.room_with_boxes(6, 3, 1, seed=3, size=20.0), scenes.room(12, size=10.0),
+           scenes.room_with_boxes(10, 8, 1, seed=9)]
+    out += scenes.batch_rooms(6, seed=77, lo=500, hi=4000)
+    extras = [None, None, {"-triangle": "1500"}, {"-triangle": "1200"}, None, None] + [None] * 6
+    return out, extras
+
+
+def test_batch_equals_single_scene(built, workdir):
+    scs, extras = _scenes()
+    preps = [_prep(sc, workdir, f"b{i}", extras[i]) for i, sc in enumerate(scs)]
+    batch = capi.Batch([p[3] for p in preps], [p[4] for p in preps], [p[2] for p in preps])
+    total, n_active, _ = batch.run()
+    assert n_active == 0
+    steps = []
+    for i, (tri, argv, o, s, t) in enumerate(preps):
+        # the same scene through the single-scene solver, from a fresh host copy
+        s2 = capi.Scene.load(tri, o)
+        t2 = capi.Octree(s2, 2)
+        s2.init()
+        s2.prepartition()
+        dv = capi.Device(s2, t2, o)
+        n, conv, _ = dv.run()
+        assert conv
+        dv.download(s2)
+        st, cv = batch.scene_stats(i)
+        assert cv and st == n, i
+        assert np.array_equal(batch.trace(i), dv.trace()), i
+        batch.download(i, s)
+        a, b = s.view(), s2.view()
+        for k in ("accB", "deltaB"):
+            assert same_bits(a[k], b[k]), (i, k)
+        steps.append(n)
+    assert len(set(steps)) > 3          # scenes converge at different iterations
+    assert total == max(steps) + 1      # the last iteration finds every scene converged
+
+
+def test_batch_chunks_and_oracle(built, workdir):
+    scs = scenes.batch_rooms(4, seed=5, lo=500, hi=3000)
+    preps = [_prep(sc, workdir, f"bc{i}") for i, sc in enumerate(scs)]
+    batch = capi.Batch([p[3] for p in preps], [p[4] for p in preps], [p[2] for p in preps])
+    for k in (1, 3, 29, 64):
+        batch.run(k)
+    batch.run()
+    for i, (tri, argv, o, s, t) in enumerate(preps):
+        ref = runner.oracle(tri, argv)
+        assert np.array_equal(batch.trace(i), runner.trace_array(ref["trace"])), i
+        batch.download(i, s)
+        v = s.view()
+        for k in ("accB", "deltaB"):
+            assert same_bits(v[k], ref["dump"][k]), (i, k)
+
+
+def test_batch_rejects_fp64_and_multi_shooter(built, workdir):
+    sc = scenes.room(4, emitter=(0.25, 0.75))
+    tri = sc.write(os.path.join(workdir, "brej.tri"))
+    o = capi.options_from_argv(sc.argv(), parallel_src=2)
+    s = capi.Scene.load(tri, o)
+    t = capi.Octree(s, 2)
+    s.init()
+    with pytest.raises(capi.RadError):
+        capi.Batch([s], [t], [o])
