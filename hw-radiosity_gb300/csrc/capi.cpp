@@ -102,7 +102,7 @@ void rad_options_default(rad_options* o) {
     o->jobs = 2;
     o->parallel_src = 1;
     o->precision = 32;
-    o->walk_cap = 1 << 20;
+    o->walk_cap = 1 << 16;
 }
 
 const char* rad_last_error(void) { return g_err.c_str(); }

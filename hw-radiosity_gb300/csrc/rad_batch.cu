@@ -54,16 +54,17 @@ struct BatchCtl {
     int work;                  // next queue item
     int n_items;               // queue length (groups of running scenes)
     int pad[2];
-    unsigned long long rays, rays_ref, cells, tris, se, prec, capped;
+    unsigned long long rays, rays_ref, cells, tris, se, prec, capped, loops;
 };
 
 template <bool COUNT>
 __device__ __forceinline__ void flush_batch(BatchCtl* bc, Cnt& c, int lane) {
-    unsigned v[7] = {c.rays, c.rays_ref, c.cells, c.tris, c.se, c.prec, c.capped};
-    unsigned long long* dst[7] = {&bc->rays, &bc->rays_ref, &bc->cells, &bc->tris, &bc->se, &bc->prec, &bc->capped};
+    unsigned v[8] = {c.rays, c.rays_ref, c.cells, c.tris, c.se, c.prec, c.capped, c.loops};
+    unsigned long long* dst[8] = {&bc->rays, &bc->rays_ref, &bc->cells, &bc->tris, &bc->se, &bc->prec, &bc->capped,
+                                  &bc->loops};
 #pragma unroll
-    for (int q = 0; q < 7; q++) {
-        if (!COUNT && q != 0 && q != 6) continue;
+    for (int q = 0; q < 8; q++) {
+        if (!COUNT && q != 0 && q != 6 && q != 7) continue;
         unsigned s = __reduce_add_sync(kFull, v[q]);
         if (lane == 0 && s) atomicAdd(dst[q], (unsigned long long)s);
     }
@@ -95,7 +96,7 @@ __global__ void __launch_bounds__(kShootThreads)
 k_batch_shoot(const SceneDesc* __restrict__ desc, SceneState* ss, const int2* __restrict__ items, BatchCtl* bc) {
     const int lane = threadIdx.x & 31;
     const int n_items = bc->n_items;
-    Cnt c = {0, 0, 0, 0, 0, 0, 0};
+    Cnt c = {0, 0, 0, 0, 0, 0, 0, 0};
     for (;;) {
         int g = 0;
         if (lane == 0) g = atomicAdd(&bc->work, 1);
@@ -438,6 +439,7 @@ int rad_batch_stats(const rad_batch* b, rad_stats* st) {
     st->se_tests = (int64_t)ctl.se;
     st->prec_steps = (int64_t)ctl.prec;
     st->walk_cap_hits = (int64_t)ctl.capped;
+    st->walk_loops = (int64_t)ctl.loops;
     int active = 0;
     for (int d : b->done) active += !d;
     st->converged = active == 0;

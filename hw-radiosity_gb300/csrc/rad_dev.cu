@@ -71,7 +71,7 @@ k_shoot(Slots<T> S, Grid<T> G, const Shooter<T>* __restrict__ shooters, State* s
     const int n_groups = (S.n + kSlotsPerWarp - 1) / kSlotsPerWarp;
     unsigned long long kk = 0;
     int ks = -1;
-    Cnt c = {0, 0, 0, 0, 0, 0, 0};
+    Cnt c = {0, 0, 0, 0, 0, 0, 0, 0};
     for (;;) {
         int g = 0;
         if (lane == 0) g = atomicAdd(&st->work, 1);
@@ -194,13 +194,14 @@ template <typename T>
 __global__ void k_ray_hit(Grid<T> G, const T* __restrict__ p, const T* __restrict__ v, const int* __restrict__ ban,
                           int n, int* __restrict__ out, State* st) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    Cnt c = {0, 0, 0, 0, 0, 0, 0};
+    Cnt c = {0, 0, 0, 0, 0, 0, 0, 0};
     if (i < n) {
         const T pp[3] = {p[3 * i], p[3 * i + 1], p[3 * i + 2]};
         const T vv[3] = {v[3 * i], v[3 * i + 1], v[3 * i + 2]};
         out[i] = walk<T, false>(G, pp, vv, ban[i], c);
     }
     if (c.capped) atomicAdd(&st->capped, (unsigned long long)c.capped);
+    if (c.loops) atomicAdd(&st->loops, (unsigned long long)c.loops);
 }
 
 template <typename T>
@@ -212,7 +213,7 @@ template <typename T>
 __global__ void k_form_factors(Slots<T> S, Grid<T> G, const Shooter<T>* __restrict__ shp, const int* __restrict__ rcv,
                                int n, T* __restrict__ ff, State* st) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    Cnt c = {0, 0, 0, 0, 0, 0, 0};
+    Cnt c = {0, 0, 0, 0, 0, 0, 0, 0};
     if (t < 3 * n) {
         const Shooter<T> s = *shp;
         const int i = rcv[t / 3], v = t % 3;
@@ -221,6 +222,7 @@ __global__ void k_form_factors(Slots<T> S, Grid<T> G, const Shooter<T>* __restri
         ff[t] = corner_ff<T, false>(s, pv, nd, nn.w, (int)fr.w, G, c);
     }
     if (c.capped) atomicAdd(&st->capped, (unsigned long long)c.capped);
+    if (c.loops) atomicAdd(&st->loops, (unsigned long long)c.loops);
 }
 
 // ------------------------------------------------------------------ no-allocation variant
@@ -244,7 +246,7 @@ template <typename T>
 __global__ void k_form_factors_many(Slots<T> S, Grid<T> G, const Shooter<T>* __restrict__ sh, int n_src,
                                     const int* __restrict__ rcv, int n_rcv, T* __restrict__ ff, State* st) {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    Cnt c = {0, 0, 0, 0, 0, 0, 0};
+    Cnt c = {0, 0, 0, 0, 0, 0, 0, 0};
     if (t < 3LL * n_rcv * n_src) {
         const int s = (int)(t / (3LL * n_rcv));
         const int rem = (int)(t - (long long)s * 3 * n_rcv);
@@ -258,6 +260,7 @@ __global__ void k_form_factors_many(Slots<T> S, Grid<T> G, const Shooter<T>* __r
         }
     }
     if (c.capped) atomicAdd(&st->capped, (unsigned long long)c.capped);
+    if (c.loops) atomicAdd(&st->loops, (unsigned long long)c.loops);
 }
 
 }  // namespace dev
@@ -732,6 +735,7 @@ int rad_dev_stats(const rad_dev* h, rad_stats* st) {
         st->se_tests = (int64_t)d.host.se;
         st->prec_steps = (int64_t)d.host.prec;
         st->walk_cap_hits = (int64_t)d.host.capped;
+        st->walk_loops = (int64_t)d.host.loops;
         st->converged = d.host.done;
         st->n_slots = d.S.n;
         st->device_bytes = (int64_t)(d.bytes + d.trace_cap * 4);

@@ -114,10 +114,10 @@ struct State {
     long long step_limit;
     long long trace_cap;
     int* trace;
-    unsigned long long rays, rays_ref, cells, tris, se, prec, capped;
+    unsigned long long rays, rays_ref, cells, tris, se, prec, capped, loops;
 };
 
-struct Cnt { unsigned rays, rays_ref, cells, tris, se, prec, capped; };
+struct Cnt { unsigned rays, rays_ref, cells, tris, se, prec, capped, loops; };
 
 // Cell coordinate along one axis: a first guess in T, corrected against the
 // thresholds so the result equals the reference's FP64 expression exactly.
@@ -133,14 +133,34 @@ __device__ __forceinline__ int cell_axis(T q, T g0, T inv, const T* th, int D) {
 // ------------------------------------------------------------------ walk
 // RayHitted (raycast.cpp:335-360) with TreeNodeNum (254-281) as a table
 // lookup, TriListHitted/TriHitted (283-333) and NextPoint (235-251).
+//
+// The walk's whole state at the top of an iteration is (t, prev): q is
+// p + t*v, and everything after depends on q and prev only.  When that state
+// repeats, the reference loops forever (it only notices one cell repeated on
+// consecutive steps).  This happens when TreeNodeNum returns a leaf that does
+// not contain q (GridNum = (int)((G1-G0)/MinGridLen) can truncate to 63 where
+// the tree is 64 cells deep, and the bit descent then picks wrong octants):
+// the exits measured from the origin can send the walk round a cycle of
+// cells, or a "Precision Exceeded" re-step at huge t leaves t unchanged.
+// Brent's cycle detection (one saved state, compared every step, replaced at
+// powers of two) finds any repeated state; the walk then stops, is counted
+// in `loops`, and the ray is treated as blocked (-3).  A walk the reference
+// finishes never repeats a state, so its result is untouched.
 template <typename T, bool COUNT>
 __device__ __forceinline__ int walk(const Grid<T>& G, const T p[3], const T v[3], int ban, Cnt& c) {
     T t = 0;
     int prev = -1;
     T q0 = p[0], q1 = p[1], q2 = p[2];
+    T chk_t = (T)-1;                   // Brent: saved state, power, steps since saved
+    int chk_prev = -2, power = 1, lam = 0;
     for (int it = 0; it < G.walk_cap; ++it) {
         if (q0 < G.g0[0] || q0 > G.g1[0] || q1 < G.g0[1] || q1 > G.g1[1] || q2 < G.g0[2] || q2 > G.g1[2])
             return -1;
+        if (t == chk_t && prev == chk_prev) {
+            c.loops++;
+            return -3;
+        }
+        if (++lam == power) { chk_t = t; chk_prev = prev; power <<= 1; lam = 0; }
         if (COUNT) c.cells++;
         // (int)(((double)q - G0) / MinGridLen) per axis, found exactly from the thresholds
         const int gx = cell_axis(q0, G.g0[0], G.inv_grid, G.thr + G.thr_off[0], G.dims[0]);
@@ -267,12 +287,12 @@ __device__ __forceinline__ void warp_max(unsigned long long& k, int& i) {
 
 template <bool COUNT>
 __device__ __forceinline__ void flush_counters(State* st, Cnt& c, int lane) {
-    unsigned v[7] = {c.rays, c.rays_ref, c.cells, c.tris, c.se, c.prec, c.capped};
-    unsigned long long* dst[7] = {&st->rays, &st->rays_ref, &st->cells, &st->tris, &st->se, &st->prec, &st->capped};
-    const int nc = COUNT ? 7 : 1;
+    unsigned v[8] = {c.rays, c.rays_ref, c.cells, c.tris, c.se, c.prec, c.capped, c.loops};
+    unsigned long long* dst[8] = {&st->rays, &st->rays_ref, &st->cells, &st->tris, &st->se, &st->prec, &st->capped,
+                                  &st->loops};
 #pragma unroll
-    for (int q = 0; q < 7; q++) {
-        if (q >= nc && q != 6) continue;
+    for (int q = 0; q < 8; q++) {
+        if (!COUNT && q != 0 && q != 6 && q != 7) continue;
         unsigned s = __reduce_add_sync(kFull, v[q]);
         if (lane == 0 && s) atomicAdd(dst[q], (unsigned long long)s);
     }
@@ -464,7 +484,7 @@ inline Grid<T> grid_params(const Octree<T>& o, int walk_cap) {
     G.t_eps = o.t_eps;
     G.v_eps = o.v_eps;
     G.n_thr = (int)o.thr.size();
-    G.walk_cap = walk_cap > 0 ? walk_cap : (1 << 20);
+    G.walk_cap = walk_cap > 0 ? walk_cap : (1 << 16);
     return G;
 }
 

@@ -50,7 +50,8 @@ typedef struct rad_options {
     int32_t parallel_src;   /* -parallel_src ParallelSource = 1 (shooters per step) */
     /* extensions */
     int32_t precision;      /* 32: FP32 solver (reference FP32 build); 64: all-FP64 form */
-    int32_t walk_cap;       /* max cell steps per visibility walk (default 1<<20) */
+    int32_t walk_cap;       /* max cell steps per visibility walk (default 65536; a walk of the
+                               reference crosses at most a few hundred cells) */
 } rad_options;
 
 typedef struct rad_scene rad_scene;   /* host scene store */
@@ -95,6 +96,8 @@ typedef struct rad_stats {
     int32_t converged;      /* 1 once a selection found no candidate */
     int32_t n_slots;
     int64_t device_bytes;   /* device memory held by the handle */
+    int64_t walk_loops;     /* walks stopped because their state repeated: the reference's
+                               RayHitted never returns on these (ray treated as blocked) */
 } rad_stats;
 
 void rad_options_default(rad_options* o);

@@ -355,14 +355,28 @@ static int cell_hit(const real *p, const real *v, int at, int ban) {
     return best;
 }
 
-/* src/raycast.cpp:335-360 */
+/* src/raycast.cpp:335-360.  The walk's state at the top of the loop is
+ * (t, prev).  When it repeats, the reference's loop never ends (it only
+ * notices one cell repeated on consecutive steps); this happens when
+ * TreeNodeNum returns a leaf that does not contain q (GridNum truncated to 63
+ * where the tree is 64 cells deep).  Brent's cycle detection finds any
+ * repeated state; such a walk stops here and the ray counts as blocked (-3),
+ * recorded in cnt_loops.  Walks the reference finishes are unaffected. */
+static long long cnt_loops;
 static int ray_hit(const real *p, const real *v, int from, int target) {
     (void)target;
     cnt_rays++;
     real t = 0;
     int prev = -1, cur, hit;
     vec3 q = {p[0], p[1], p[2]};
+    real chk_t = -1;
+    int chk_prev = -2, power = 1, lam = 0;
     while ((cur = cell_of(q)) >= 0) {
+        if (t == chk_t && prev == chk_prev) {
+            cnt_loops++;
+            return -3;
+        }
+        if (++lam == power) { chk_t = t; chk_prev = prev; power <<= 1; lam = 0; }
         cnt_cells++;
         if (prev == cur) {
             cnt_prec++;
@@ -1095,8 +1109,8 @@ int main(int argc, char **argv) {
     if (trace) fclose(trace);
     const char *dump = getenv("RAD_DUMP");
     if (dump) put_dump(dump, steps);
-    fprintf(stderr, "[COUNT] rays %lld cells %lld tri_tests %lld se_tests %lld prec %lld\n", cnt_rays, cnt_cells,
-            cnt_tris, cnt_se, cnt_prec);
+    fprintf(stderr, "[COUNT] rays %lld cells %lld tri_tests %lld se_tests %lld prec %lld loops %lld\n", cnt_rays,
+            cnt_cells, cnt_tris, cnt_se, cnt_prec, cnt_loops);
     fprintf(stderr, "[INFO] Shooting took %f sec for %d steps\n", t3 - t2, steps);
     return 0;
 }

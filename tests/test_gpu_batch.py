@@ -85,3 +85,24 @@ def test_batch_rejects_fp64_and_multi_shooter(built, workdir):
     s.init()
     with pytest.raises(capi.RadError):
         capi.Batch([s], [t], [o])
+
+
+def test_walks_the_reference_never_finishes(built, workdir):
+    """Scene 27 of the 256-room batch: the reference's TreeNodeNum returns leaves
+    that do not contain the point (GridNum truncates to 63), and tens of
+    thousands of walks cycle forever in the reference.  The solver and the
+    oracle both stop a walk whose (t, prev) state repeats and treat the ray as
+    blocked; they must agree bit for bit."""
+    g = scenes.batch_rooms(28, seed=4000)[27]
+    tri, argv, o, s, t = _prep(g, workdir, "loop27")
+    dv = capi.Device(s, t, o)
+    n, conv, _ = dv.run(6)
+    assert n == 6
+    dv.download(s)
+    assert dv.stats()["walk_loops"] > 1000
+    ref = runner.oracle(tri, argv, steps=6)
+    assert runner.counters(ref["stderr"])["loops"] > 1000
+    assert np.array_equal(dv.trace(), runner.trace_array(ref["trace"]))
+    v = s.view()
+    for k in ("accB", "deltaB"):
+        assert same_bits(v[k], ref["dump"][k]), k

@@ -135,3 +135,12 @@ def test_cell_thresholds_equal_reference_expression(built, workdir, fp64):
             assert np.array_equal(ref, fast)
             assert np.array_equal(r2, f2)
             assert ref.min() >= 0 and ref.max() <= tree.info()["dims"][axis] - 1
+
+
+def test_oracle_terminates_on_cycling_walks(built, workdir):
+    """The reference loops forever on some walks of batch scene 27; the oracle
+    (and the solver) stop them by detecting a repeated walk state."""
+    g = scenes.batch_rooms(28, seed=4000)[27]
+    tri = g.write(os.path.join(workdir, "cyc27.tri"))
+    r = runner.oracle(tri, g.argv(), steps=3, timeout=120)
+    assert runner.counters(r["stderr"])["loops"] > 0
