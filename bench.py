@@ -216,6 +216,53 @@ def measure_batched(capi, n_scenes, warmup, iters, device):
             "l2": "batch inputs exceed L2; plain timed without flush (graph chunks)"}
 
 
+def rank_env():
+    return (int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0")),
+            int(os.environ.get("LOCAL_RANK", "0")))
+
+
+class Ranks:
+    """Replicas only: one solver per GPU, no data exchange.  The only
+    collectives are the contract's barrier around the timed region and the
+    maximum of the ranks' times (the whole job ends with the slowest rank)."""
+
+    def __init__(self, world, backend):
+        import torch
+        self.torch = torch
+        self.dist = None
+        self.cuda = backend == "nccl"
+        if world > 1:
+            import torch.distributed as dist
+            dist.init_process_group(backend)
+            self.dist = dist
+
+    def sync(self):
+        if self.cuda:
+            self.torch.cuda.synchronize()
+
+    def barrier(self):
+        self.sync()
+        if self.dist:
+            self.dist.barrier()
+        self.sync()
+
+    def max(self, x):
+        if not self.dist:
+            return x
+        t = self.torch.tensor([x], dtype=self.torch.float64, device="cuda" if self.cuda else "cpu")
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.dist:
+            self.dist.destroy_process_group()
+
+
+def replica_value(world, steps_per_rank, worst_ms):
+    """Whole-job shots/s: every rank shoots its own replica."""
+    return world * steps_per_rank / (worst_ms / 1000.0) if worst_ms > 0 else None
+
+
 def run_reference_arm(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -257,27 +304,11 @@ def main():
     import torch
     from hwrad import capi
 
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
+    world, rank, local = rank_env()
     torch.cuda.set_device(local)
-    dist = None
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl")
-
-    def barrier():
-        torch.cuda.synchronize()
-        if dist:
-            dist.barrier()
-        torch.cuda.synchronize()
-
-    def max_over_ranks(x):
-        if not dist:
-            return x
-        t = torch.tensor([x], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+    ranks = Ranks(world, "nccl")
+    barrier, max_over_ranks = ranks.barrier, ranks.max
+    dist = ranks.dist
 
     log("config-2 scene: host preparation")
     tmp = tempfile.mkdtemp(prefix="radbench_")
@@ -369,7 +400,7 @@ def main():
         with open(tp) as fh:
             traffic = json.load(fh).get("dram_bytes_per_launch")
 
-    value = world * done / (worst_ms / 1000.0) if worst_ms > 0 else None
+    value = replica_value(world, done, worst_ms)
     h2d = 0
     # the upload: slot records (6 x 16 B per slot, 3 of them x3) + octree; approximated by device bytes held
     h2d = dev_bytes / max(args.warmup + done, 1)
@@ -411,14 +442,13 @@ def main():
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "note": "rad_dev_create (upload) + run + rad_dev_download over warm-up + timed steps"},
         "batched": batched,
-        "gpu_launches": 2 * done,
+        "gpu_launches": done if opts.parallel_src <= 1 else 2 * done,
         "clocks": clocks.summary(),
         "cpu_baseline": cpu,
     }
     if rank == 0:
         print(json.dumps(line))
-    if dist:
-        dist.destroy_process_group()
+    ranks.close()
     return 0
 
 

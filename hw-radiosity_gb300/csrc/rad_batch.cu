@@ -91,8 +91,11 @@ __global__ void k_batch_setup(const SceneDesc* __restrict__ desc, SceneState* ss
     st.steps += 1;
 }
 
+#ifndef RAD_SHOOT_MIN_BLOCKS
+#define RAD_SHOOT_MIN_BLOCKS 3
+#endif
 template <bool COUNT>
-__global__ void __launch_bounds__(kShootThreads)
+__global__ void __launch_bounds__(kShootThreads, RAD_SHOOT_MIN_BLOCKS)
 k_batch_shoot(const SceneDesc* __restrict__ desc, SceneState* ss, const int2* __restrict__ items, BatchCtl* bc) {
     const int lane = threadIdx.x & 31;
     const int n_items = bc->n_items;

@@ -45,9 +45,17 @@ namespace dev {
 // Persistent: each warp takes 10-slot groups from the step's queue until it
 // is empty, so warps that finish early take more work; the CTA's (key, slot)
 // maximum is written by whichever of its warps finishes last.
-template <typename T, bool COUNT>
-__global__ void __launch_bounds__(kShootThreads)
-k_shoot(Slots<T> S, Grid<T> G, const Shooter<T>* __restrict__ shooters, State* st, Partial* __restrict__ part, T conv) {
+//
+// FUSED (one shooter per step): the last warp of the whole grid to finish
+// also does the next step's selection -- it reduces the per-CTA partials,
+// builds the next shooter record and advances the step -- so a step is one
+// kernel.  Several shooters per step keep the separate k_setup.
+#ifndef RAD_SHOOT_MIN_BLOCKS
+#define RAD_SHOOT_MIN_BLOCKS 3
+#endif
+template <typename T, bool COUNT, bool FUSED>
+__global__ void __launch_bounds__(kShootThreads, RAD_SHOOT_MIN_BLOCKS)
+k_shoot(Slots<T> S, Grid<T> G, Shooter<T>* shooters, State* st, Partial* __restrict__ part, T conv) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ unsigned long long wkey[kShootThreads / 32];
     __shared__ int wslot[kShootThreads / 32];
@@ -81,20 +89,54 @@ k_shoot(Slots<T> S, Grid<T> G, const Shooter<T>* __restrict__ shooters, State* s
     }
     warp_max(kk, ks);
     flush_counters<COUNT>(st, c, lane);
+    int last = 0;
     if (lane == 0) {
         wkey[wid] = kk;
         wslot[wid] = ks;
         __threadfence_block();
-        if (atomicAdd(&ndone, 1) == kShootThreads / 32 - 1) {
-            volatile unsigned long long* vk = wkey;
-            volatile int* vs = wslot;
-            unsigned long long bk = 0;
-            int bs = -1;
-            for (int w = 0; w < kShootThreads / 32; w++)
-                if (part_less(bk, bs, vk[w], vs[w])) { bk = vk[w]; bs = vs[w]; }
-            part[blockIdx.x].key = bk;
-            part[blockIdx.x].slot = bs;
+        last = atomicAdd(&ndone, 1) == kShootThreads / 32 - 1;
+    }
+    if (!__shfl_sync(kFull, last, 0)) return;
+    // the CTA's last warp: the CTA partial
+    if (lane == 0) {
+        volatile unsigned long long* vk = wkey;
+        volatile int* vs = wslot;
+        unsigned long long bk = 0;
+        int bs = -1;
+        for (int w = 0; w < kShootThreads / 32; w++)
+            if (part_less(bk, bs, vk[w], vs[w])) { bk = vk[w]; bs = vs[w]; }
+        part[blockIdx.x].key = bk;
+        part[blockIdx.x].slot = bs;
+    }
+    if (!FUSED) return;
+    __threadfence();
+    last = 0;
+    if (lane == 0) last = atomicAdd(&st->ctas_done, 1) == (int)gridDim.x - 1;
+    if (!__shfl_sync(kFull, last, 0)) return;
+    // the grid's last warp: select the next step's shooter (listCanditate for one shooter)
+    __threadfence();
+    kk = 0;
+    ks = -1;
+    for (int q = lane; q < (int)gridDim.x; q += 32) {
+        const unsigned long long qk = __ldcg(&part[q].key);
+        const int qs = __ldcg(&part[q].slot);
+        if (part_less(kk, ks, qk, qs)) { kk = qk; ks = qs; }
+    }
+    warp_max(kk, ks);
+    if (lane == 0) {
+        long long steps = st->steps + (nsh > 0 ? 1 : 0);    // the step just shot is complete
+        if (!kk) {
+            st->done = 1;
+            st->nsh = 0;
+        } else {
+            build_shooter(S, ks, shooters[0]);
+            if (steps < st->trace_cap) st->trace[steps] = ks;
+            st->nsh = 1;
+            if (steps >= st->step_limit) st->paused = 1;
         }
+        st->steps = steps;
+        st->work = 0;
+        st->ctas_done = 0;
     }
 }
 
@@ -368,13 +410,15 @@ int upload(const Scene<T>& s, const Octree<T>& o, const rad_options& opt, int de
     // per-step state; k_shoot is persistent: as many CTAs as fit at once
     d.n_thr = (int)o.thr.size();
     if (d.shoot_smem() > 48 * 1024) {
-        CU(cudaFuncSetAttribute(k_shoot<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)d.shoot_smem()));
-        CU(cudaFuncSetAttribute(k_shoot<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)d.shoot_smem()));
+        CU(cudaFuncSetAttribute(k_shoot<T, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)d.shoot_smem()));
+        CU(cudaFuncSetAttribute(k_shoot<T, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)d.shoot_smem()));
+        CU(cudaFuncSetAttribute(k_shoot<T, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)d.shoot_smem()));
+        CU(cudaFuncSetAttribute(k_shoot<T, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)d.shoot_smem()));
     }
     {
         int sms = 0, per_sm = 0;
         CU(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
-        CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_shoot<T, false>, kShootThreads, d.shoot_smem()));
+        CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_shoot<T, false, true>, kShootThreads, d.shoot_smem()));
         const int n_groups = (n + kSlotsPerWarp - 1) / kSlotsPerWarp;
         const int want = (n_groups + kShootThreads / 32 - 1) / (kShootThreads / 32);
         d.n_cta = std::max(1, std::min(want, std::max(1, sms * per_sm)));
@@ -392,20 +436,33 @@ int upload(const Scene<T>& s, const Octree<T>& o, const rad_options& opt, int de
     CU(cudaMemsetAsync(d.d_shooters, 0, sizeof(Shooter<T>) * d.P, d.stream));
     CU(cudaMemsetAsync(d.d_part, 0, sizeof(Partial) * d.n_cta, d.stream));
     // initial selection keys: a step with no shooter only reduces the keys
-    k_shoot<T, false><<<d.n_cta, kShootThreads, d.shoot_smem(), d.stream>>>(d.S, d.G, d.d_shooters, d.d_state, d.d_part, d.conv);
+    launch_shoot(d, d.stream);
     CU(cudaGetLastError());
+    CU(cudaStreamSynchronize(d.stream));
+    CU(cudaMemcpyAsync(&st, d.d_state, sizeof st, cudaMemcpyDeviceToHost, d.stream));
     CU(cudaStreamSynchronize(d.stream));
     d.host = st;
     return RAD_OK;
 }
 
+// the shooting kernel of one step; with one shooter per step it also selects the next
+template <typename T>
+void launch_shoot(DevImpl<T>& d, cudaStream_t s) {
+    const bool fused = d.P == 1;
+    if (d.counting && fused)
+        k_shoot<T, true, true><<<d.n_cta, kShootThreads, d.shoot_smem(), s>>>(d.S, d.G, d.d_shooters, d.d_state, d.d_part, d.conv);
+    else if (d.counting)
+        k_shoot<T, true, false><<<d.n_cta, kShootThreads, d.shoot_smem(), s>>>(d.S, d.G, d.d_shooters, d.d_state, d.d_part, d.conv);
+    else if (fused)
+        k_shoot<T, false, true><<<d.n_cta, kShootThreads, d.shoot_smem(), s>>>(d.S, d.G, d.d_shooters, d.d_state, d.d_part, d.conv);
+    else
+        k_shoot<T, false, false><<<d.n_cta, kShootThreads, d.shoot_smem(), s>>>(d.S, d.G, d.d_shooters, d.d_state, d.d_part, d.conv);
+}
+
 template <typename T>
 int launch_step(DevImpl<T>& d, cudaStream_t s) {
-    k_setup<T><<<1, kSetupThreads, 0, s>>>(d.S, d.d_shooters, d.d_state, d.d_part, d.n_cta, d.conv, d.P);
-    if (d.counting)
-        k_shoot<T, true><<<d.n_cta, kShootThreads, d.shoot_smem(), s>>>(d.S, d.G, d.d_shooters, d.d_state, d.d_part, d.conv);
-    else
-        k_shoot<T, false><<<d.n_cta, kShootThreads, d.shoot_smem(), s>>>(d.S, d.G, d.d_shooters, d.d_state, d.d_part, d.conv);
+    if (d.P > 1) k_setup<T><<<1, kSetupThreads, 0, s>>>(d.S, d.d_shooters, d.d_state, d.d_part, d.n_cta, d.conv, d.P);
+    launch_shoot(d, s);
     CU(cudaGetLastError());
     return RAD_OK;
 }
@@ -477,12 +534,9 @@ int run(DevImpl<T>& d, long long max_steps, long long* done_steps, int* converge
         if (mode == 2) {
             // one step per iteration, kernels timed separately
             CU(cudaEventRecord(d.ev[0], d.stream));
-            k_setup<T><<<1, kSetupThreads, 0, d.stream>>>(d.S, d.d_shooters, d.d_state, d.d_part, d.n_cta, d.conv, d.P);
+            if (d.P > 1) k_setup<T><<<1, kSetupThreads, 0, d.stream>>>(d.S, d.d_shooters, d.d_state, d.d_part, d.n_cta, d.conv, d.P);
             CU(cudaEventRecord(d.ev[1], d.stream));
-            if (d.counting)
-                k_shoot<T, true><<<d.n_cta, kShootThreads, d.shoot_smem(), d.stream>>>(d.S, d.G, d.d_shooters, d.d_state, d.d_part, d.conv);
-            else
-                k_shoot<T, false><<<d.n_cta, kShootThreads, d.shoot_smem(), d.stream>>>(d.S, d.G, d.d_shooters, d.d_state, d.d_part, d.conv);
+            launch_shoot(d, d.stream);
             CU(cudaGetLastError());
             CU(cudaEventRecord(d.ev[2], d.stream));
         } else {

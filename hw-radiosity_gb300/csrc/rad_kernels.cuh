@@ -106,6 +106,7 @@ __host__ __device__ inline size_t kMaxShooterBytes(int nsh) {
 
 struct State {
     int work;               // next 10-slot group of the current step (k_shoot queue)
+    int ctas_done;          // CTAs of the current k_shoot that have finished (fused selection)
     int done;               // a selection found no candidate
     int paused;             // step limit reached
     int nsh;                // shooters of the current step
@@ -179,11 +180,14 @@ __device__ __forceinline__ int walk(const Grid<T>& G, const T p[3], const T v[3]
         const int b = cr.y, e = cr.z;
         T tmin = (T)1000000.0;
         int best = -1;
+        // the next entry's (n, id) and (c) records are in flight while this one is tested
+        Q4<T> nx_en = {0, 0, 0, 0}, nx_ec = {0, 0, 0, 0};
+        if (b < e) { nx_en = G.entry[5 * b]; nx_ec = G.entry[5 * b + 1]; }
         for (int k = b; k < e; ++k) {
-            const Q4<T> en = G.entry[5 * k];
+            const Q4<T> en = nx_en, ec = nx_ec;
+            if (k + 1 < e) { nx_en = G.entry[5 * (k + 1)]; nx_ec = G.entry[5 * (k + 1) + 1]; }
             const int id = real_to_int(en.w);
             if (id == ban) continue;
-            const Q4<T> ec = G.entry[5 * k + 1];
             if (COUNT) c.tris++;
             const T a1 = v[0] * en.x + v[1] * en.y + v[2] * en.z;
             const T w0 = ec.x - p[0], w1 = ec.y - p[1], w2 = ec.z - p[2];

@@ -55,17 +55,12 @@ class Scene:
         return int(self.vtx.shape[0])
 
     def to_tri(self) -> str:
-        """Render as ``.tri`` text; coordinates printed exactly (float32 repr)."""
-        out: List[str] = []
-        v = self.vtx.astype(np.float32)
-        for i in range(self.n):
-            f = self.frgb[i]
-            b = self.brgb[i]
-            out.append("Triangle \n")
-            out.append(f"{f[0]} {f[1]} {f[2]} {b[0]} {b[1]} {b[2]}\n")
-            for k in range(3):
-                out.append(" ".join(_fmt(x) for x in v[i, k]) + "\n")
-        return "".join(out)
+        """Render as ``.tri`` text.  Coordinates are printed with 9 significant
+        digits, which parse back to the same float32 values."""
+        v = self.vtx.astype(np.float32).astype(np.float64).reshape(-1, 9).tolist()
+        c = np.concatenate([self.frgb, self.brgb], axis=1).astype(np.int64).tolist()
+        blk = "Triangle \n%d %d %d %d %d %d\n%.9g %.9g %.9g\n%.9g %.9g %.9g\n%.9g %.9g %.9g\n"
+        return "".join(blk % (tuple(ci) + tuple(vi)) for ci, vi in zip(c, v))
 
     def write(self, path: str) -> str:
         with open(path, "w") as fh:
@@ -82,12 +77,6 @@ class Scene:
             if val is not None:
                 args.append(str(val))
         return args
-
-
-def _fmt(x: np.float32) -> str:
-    # shortest text that parses back to the same float32
-    s = np.format_float_positional(np.float32(x), unique=True, trim="-")
-    return s
 
 
 def concat(scenes: Sequence[Scene], options: Dict[str, str], name: str) -> Scene:
