@@ -395,10 +395,11 @@ def main():
     peak, peak_kind = _peaks()
     achieved = per_launch / avg_shoot_s / 1e9 if avg_shoot_s > 0 else None
     traffic = None
-    tp = os.path.join(REPO, "profiles", "k_shoot_traffic.json")
+    tp = os.path.join(REPO, "profiles", "k_shoot_room64_boxes16.traffic.txt")
     if os.path.exists(tp):
-        with open(tp) as fh:
-            traffic = json.load(fh).get("dram_bytes_per_launch")
+        for line in open(tp):
+            if line.startswith("dram_bytes_per_launch:"):
+                traffic = int(line.split(":")[1])
 
     value = replica_value(world, done, worst_ms)
     h2d = 0
