@@ -871,6 +871,122 @@ static int shoot_step(FILE *trace) {
     return 1;
 }
 
+/* ---------------------------------------------------------------- adaptive variant */
+/* The reference built with include/config.h = ADAPT + ROLLBACK only: no
+ * pre-partition, serialRadiosity (rad.cpp:452-490) and the full Shade
+ * (shade.cpp:435-554) whose delta-FF test can split a receiver. */
+static int variant_adapt = 0;
+
+/* glibc rand(): TYPE_3 additive feedback generator, seeded with 1 (the
+ * reference never calls srand).  r[0] = 1; r[i] = 16807 r[i-1] mod (2^31-1)
+ * for i < 31 (Schrage's method); r[i] = r[i-31] for i = 31..33;
+ * r[i] = r[i-31] + r[i-3] (mod 2^32) after that; output k is r[k+344] >> 1. */
+static uint32_t rs_r[34];
+static int rs_i, rs_init;
+static int glibc_rand(void) {
+    if (!rs_init) {
+        int32_t w = 1;
+        rs_r[0] = 1;
+        for (int i = 1; i < 31; i++) {
+            int32_t hi = w / 127773, lo = w % 127773;
+            w = 16807 * lo - 2836 * hi;
+            if (w < 0) w += 2147483647;
+            rs_r[i] = (uint32_t)w;
+        }
+        for (int i = 31; i < 34; i++) rs_r[i] = rs_r[i - 31];
+        rs_i = 34;
+        rs_init = 1;
+        for (int k = 0; k < 310; k++) glibc_rand();
+    }
+    /* ring of 34: r[i] = r[i-31] + r[i-3] */
+    uint32_t v = rs_r[(rs_i - 31) % 34] + rs_r[(rs_i - 3) % 34];
+    rs_r[rs_i % 34] = v;
+    rs_i++;
+    return (int)(v >> 1);
+}
+
+/* src/shade.cpp:49-68 */
+static real sample_point(const tri_t *t, real *pt, const real ff[3]) {
+    real r1 = (real)glibc_rand(), r2 = (real)glibc_rand(), r3 = (real)glibc_rand();
+    real tot = r1 + r2 + r3;
+    r1 /= tot; r2 /= tot; r3 /= tot;
+    for (int v = 0; v < 3; v++) pt[v] = r1 * t->p[0][v] + r2 * t->p[1][v] + r3 * t->p[2][v];
+    return r1 * ff[0] + r2 * ff[1] + r3 * ff[2];
+}
+
+static real corner_ff_at(const tri_t *src, int logsrc, const tri_t *des, int logdes, const real *pt) {
+    patch_t sp;
+    as_patch(src, &sp);
+    return adapt_ff(point_ff(&sp, logsrc, des, logdes, pt), &sp, logsrc, des, logdes, pt);
+}
+
+static real fabs_f(real x) { return (real)fabs((double)x); }   /* ffabs, rad.h:14 */
+
+/* src/shade.cpp:435-554 with ADAPT, ROLLBACK, no DONT_PARTITION, no PARALLEL.
+ * The shooter is read from its slot each time (a split can replace it). */
+static int shade_adapt(int src_id, int logsrc, int des_id, int logdes) {
+    real ff[3];
+    for (int v = 0; v < 3; v++) ff[v] = corner_ff_at(&T[src_id], logsrc, &T[des_id], logdes, T[des_id].p[v]);
+    tri_t *des = &T[des_id];
+    if (des->area < AreaLimit) { deposit(&T[src_id], des, ff); return 0; }
+    if (pool_full(4) || (double)des->area < 1e-8) { deposit(&T[src_id], des, ff); return 0; }
+    real ground = (real)((double)(ff[0] + ff[1] + ff[2]) / 3.0);
+    real ffs = corner_ff_at(&T[src_id], logsrc, des, logdes, des->c);
+    real dff;
+    if ((dff = fabs_f(ground - ffs)) < DeltaFFLimit) {
+        int n = (int)(des->area / SampleArea);
+        for (int k = 0; k < n; k++) {
+            real pt[3];
+            ground = sample_point(des, pt, ff);
+            ffs = corner_ff_at(&T[src_id], logsrc, des, logdes, pt);
+            if ((dff = fabs_f(ground - ffs)) > DeltaFFLimit) break;
+        }
+        if (dff < DeltaFFLimit) { deposit(&T[src_id], des, ff); return 0; }
+    }
+    int out[4], reshade;
+    int rep = split_and_store(des_id, out, &reshade);
+    if (reshade) {
+        tri_t *t4 = &T[out[3]];
+        for (int v = 0; v < 3; v++) ff[v] = corner_ff_at(&T[src_id], logsrc, t4, logdes, t4->p[v]);
+        deposit(&T[src_id], t4, ff);
+    }
+    return rep;
+}
+
+/* src/rad.cpp:359-386: the first strict maximum (ties: lowest index) */
+static int max_delta_rad(void) {
+    int best = -1;
+    real m = 0;
+    for (int i = 0; i < trinum; i++) {
+        if (T[i].parent < 0) continue;
+        real d = T[i].deltaB[0] + T[i].deltaB[1] + T[i].deltaB[2];
+        if (d > m && d > ConvergeLimit) { best = i; m = d; }
+    }
+    return best;
+}
+
+/* src/rad.cpp:452-490 */
+static int serial_step(FILE *trace) {
+    int src = max_delta_rad();
+    if (trace) {
+        if (src >= 0) fprintf(trace, "1 %d\n", src);
+        else fputs("0\n", trace);
+    }
+    if (src < 0) return 0;
+    const int logsrc = T[src].parent;
+    for (int d = 0; d < trinum; d++) {
+        if (d == src) continue;
+        if (T[d].parent < 0) continue;
+        int open = 0;
+        for (int v = 0; v < 3; v++)
+            for (int c = 0; c < 3; c++) open |= ((double)T[d].accB[v][c] < 255.0);
+        if (!open) continue;
+        if (shade_adapt(src, logsrc, d, T[d].parent)) d--;
+    }
+    T[src].deltaB[0] = T[src].deltaB[1] = T[src].deltaB[2] = 0;
+    return 1;
+}
+
 /* ---------------------------------------------------------------- output */
 /* Float to text as include/float2string.h does it (fixed point, up to 8
  * truncated fraction digits, trailing zeros dropped).  Returns 0 and leaves
@@ -1055,7 +1171,11 @@ int main(int argc, char **argv) {
         int j, has = 0;
         for (j = 0; j < 13; j++)
             if (!strcmp(argv[i], opts[j])) { has = 1; break; }
-        if (!has) { in = argv[i]; continue; }
+        if (!has) {
+            if (!strcmp(argv[i], "-adaptive")) { variant_adapt = 1; continue; }
+            in = argv[i];
+            continue;
+        }
         int ok = 1, dummy;
         switch (j) {
         case 0: ok = i + 1 < argc && sscanf(argv[++i], "%d", &opt_debug) == 1; break;
@@ -1089,14 +1209,14 @@ int main(int argc, char **argv) {
     long max_steps = getenv("RAD_MAX_STEPS") ? atol(getenv("RAD_MAX_STEPS")) : -1;
 
     init_radiosity();
-    pre_partition();
+    if (!variant_adapt) pre_partition();
     run_queries();
     double t2 = now_s();
     int loop, steps = 0;
     for (loop = 1;; loop++) {
         if (WriteIteration && loop % WriteIteration == 0) fprintf(stderr, "[INFO] Loop %d BEGIN\n", loop);
         if (max_steps >= 0 && steps >= max_steps) break;
-        if (!shoot_step(trace)) break;
+        if (!(variant_adapt ? serial_step(trace) : shoot_step(trace))) break;
         steps++;
         if (WriteIteration && loop % WriteIteration == 0) {
             write_fin(out, loop);

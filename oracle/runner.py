@@ -21,6 +21,7 @@ ORACLE64 = os.path.join(HERE, "_build", "radoracle64")
 REF32 = os.path.join(HERE, "_ref", "rad_ref32")
 REF32C = os.path.join(HERE, "_ref", "rad_ref32c")
 REF64 = os.path.join(HERE, "_ref", "rad_ref64")
+REF32A = os.path.join(HERE, "_ref", "rad_ref32a")
 
 
 def build_oracle() -> None:
@@ -63,8 +64,10 @@ def run(binary: str, tri: str, args: Sequence[str], steps: Optional[int] = None,
             "fin": fin, "stderr": r.stderr, "stdout": r.stdout, "dir": wd}
 
 
-def oracle(tri: str, args: Sequence[str], steps: Optional[int] = None, fp64: bool = False, **kw):
-    return run(ORACLE64 if fp64 else ORACLE32, tri, args, steps, **kw)
+def oracle(tri: str, args: Sequence[str], steps: Optional[int] = None, fp64: bool = False, adaptive: bool = False,
+           **kw):
+    """The C restatement; adaptive=True runs the adaptive split variant."""
+    return run(ORACLE64 if fp64 else ORACLE32, tri, list(args) + (["-adaptive"] if adaptive else []), steps, **kw)
 
 
 def rays(tri: str, args: Sequence[str], p: np.ndarray, v: np.ndarray, ban: np.ndarray, fp64: bool = False) -> np.ndarray:

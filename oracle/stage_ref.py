@@ -23,6 +23,10 @@ behaviour-preserving patch set so the binary can be used as a checker:
    tests, "Precision Exceeded" re-steps) that compile to nothing unless
    ``RAD_COUNTERS`` is defined.
 
+A third copy, ``oracle/_ref/src_adapt/``, replaces ``include/config.h`` by
+ADAPT + ROLLBACK only: the adaptive split variant (serial loop, delta-FF split
+test, no pre-partition).
+
 ``--fp64`` additionally rewrites ``float`` to ``double`` in the solver's data
 types and arithmetic (vector.h, rad.h, shade.cpp, raycast.cpp and the rad.cpp
 locals), keeping the command-line option globals as ``float`` and formatting
@@ -64,6 +68,10 @@ def _patch_common(files):
     rc = _sub_once(rc, "\tvector<int> C(listCanditate());\n",
                    "\tvector<int> C(listCanditate());\n\tif (rad_hook_shot(C)) return 0;\n",
                    "hook call")
+    rc = _sub_once(rc, "\tphysrc = MaxDeltaRad();\n",
+                   "\tphysrc = MaxDeltaRad();\n\t{ vector<int> C_; if (physrc >= 0) C_.push_back(physrc);"
+                   " if (rad_hook_shot(C_)) return 0; }\n",
+                   "serial hook call")
     files["src/rad.cpp"] = rc
 
     ry = files["src/raycast.cpp"]
@@ -144,7 +152,13 @@ def main():
         with open(os.path.join(args.ref, n)) as f:
             files[n] = f.read()
     files = _patch_common(files)
-    for sub, fs in (("src", files), ("src64", _to_fp64(files))):
+    # the adaptive split variant: include/config.h with ADAPT and ROLLBACK only
+    # (serialRadiosity, the full Shade with its delta-FF split test, no
+    # pre-partition) -- the configuration in which the split path is live
+    adapt = dict(files)
+    adapt["include/config.h"] = ("#ifndef _CONFIG_H\n#define _CONFIG_H\n"
+                                 "#define ADAPT\n#define ROLLBACK\n#endif\n")
+    for sub, fs in (("src", files), ("src64", _to_fp64(files)), ("src_adapt", adapt)):
         root = os.path.join(args.out, sub)
         if os.path.isdir(root):
             shutil.rmtree(root)

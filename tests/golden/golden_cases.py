@@ -20,6 +20,12 @@ CASES = {
     "room8_p3": {"scene": ("room", {"q": 8}), "extra": {"-parallel_src": "3"}},
     # the reference's float->double build
     "room8_fp64": {"scene": ("room", {"q": 8}), "fp64": True},
+    # the adaptive split variant (config.h = ADAPT + ROLLBACK): the room at x6
+    # scale has receivers above -adapt_area 5 that the delta-FF test splits
+    "adapt_room": {"scene": ("room", {"q": 4, "size": 60.0, "emitter": (0.25, 0.75)}),
+                   "extra": {"-triangle": "1500", "-converge": "10"}, "adaptive": True},
+    "adapt_boxes": {"scene": ("room_with_boxes", {"q": 8, "n_boxes": 3, "box_q": 1, "seed": 5, "size": 40.0}),
+                    "extra": {"-triangle": "1200", "-converge": "20"}, "adaptive": True},
 }
 
 

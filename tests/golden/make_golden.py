@@ -40,15 +40,17 @@ def main():
         wd = tempfile.mkdtemp(prefix=f"golden_{name}_")
         tri = sc.write(os.path.join(wd, "scene.tri"))
         argv = sc.argv(case.get("extra"))
-        binary = runner.REF64 if case.get("fp64") else runner.REF32
-        out = runner.run(binary, tri, argv + ["-jobs", "4"], workdir=wd)
+        binary = runner.REF64 if case.get("fp64") else (runner.REF32A if case.get("adaptive") else runner.REF32)
+        # the adaptive variant is the reference's serial loop: one job
+        out = runner.run(binary, tri, argv + ["-jobs", "1" if case.get("adaptive") else "4"], workdir=wd)
         d = out["dump"]
         P = int(dict(zip(argv[::2], argv[1::2])).get("-parallel_src", 1)) if "-parallel_src" in argv else 1
         tr = runner.trace_array(out["trace"], P)
         np.savez_compressed(os.path.join(HERE, f"{name}.npz"), trace=tr, parent=d["parent"], p=d["p"],
                             accB=d["accB"], deltaB=d["deltaB"], nb=d["nb"])
         index[name] = {
-            "argv": argv, "fp64": bool(case.get("fp64")), "P": P, "n_slots": d["n"], "steps": d["steps"],
+            "argv": argv, "fp64": bool(case.get("fp64")), "adaptive": bool(case.get("adaptive")), "P": P,
+            "n_slots": d["n"], "steps": d["steps"],
             "fin_sha256": hashlib.sha256(out["fin"]).hexdigest(),
             "tri_sha256": hashlib.sha256(open(tri, "rb").read()).hexdigest(),
             "source": "reference src/ (staged by oracle/stage_ref.py), built by oracle/Makefile",

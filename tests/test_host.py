@@ -144,3 +144,22 @@ def test_oracle_terminates_on_cycling_walks(built, workdir):
     tri = g.write(os.path.join(workdir, "cyc27.tri"))
     r = runner.oracle(tri, g.argv(), steps=3, timeout=120)
     assert runner.counters(r["stderr"])["loops"] > 0
+
+
+def test_rand_restatement_equals_libc(built, workdir):
+    """The oracle's glibc rand() restatement (used by the adaptive variant's
+    sample points, shade.cpp:49-68) against the C library, seed 1."""
+    import ctypes
+    import subprocess
+    libc = ctypes.CDLL(None)
+    libc.srand(1)
+    want = [libc.rand() for _ in range(2000)]
+    src = os.path.join(workdir, "rnd.c")
+    with open(src, "w") as fh:
+        fh.write('#define main oracle_main\n#include "%s"\n#undef main\n'
+                 'int main(void){for(int i=0;i<2000;i++)printf("%%d\\n",glibc_rand());return 0;}\n'
+                 % os.path.join(runner.HERE, "radoracle.c"))
+    exe = os.path.join(workdir, "rnd")
+    subprocess.run(["gcc", "-O2", "-std=c11", "-o", exe, src, "-lm"], check=True, capture_output=True)
+    got = [int(x) for x in subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split()]
+    assert got == want

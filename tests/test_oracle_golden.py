@@ -15,7 +15,7 @@ CASES = sorted(golden_index())
 def test_oracle_matches_reference_fixture(built, workdir, name):
     tri, argv, idx = write_case(name, workdir)
     assert sha256_file(tri) == idx["tri_sha256"], "scene generator drifted from the fixture"
-    out = runner.oracle(tri, argv, fp64=idx["fp64"])
+    out = runner.oracle(tri, argv, fp64=idx["fp64"], adaptive=idx.get("adaptive", False))
     g = golden(name)
     assert np.array_equal(runner.trace_array(out["trace"], idx["P"]), g["trace"])
     d = out["dump"]
