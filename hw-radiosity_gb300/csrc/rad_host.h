@@ -86,6 +86,13 @@ template <typename T> void prepartition(Scene<T>& s);                // src/shad
 template <typename T> int write_fin(const Scene<T>& s, const char* prefix, int loop, std::string& err);
 template <typename T> void build_octree(const Scene<T>& s, Octree<T>& o, int threads);  // raycast.cpp:216-233
 
+// PartitionTriangleAndStore (shade.cpp:311-431) on receiver slot sid: out[]
+// gets t1..t4 (-1 where not created), *nbid the neighbour split with it (-1
+// for none); returns -1 (no split), 0, or 1 (sid now holds a child).
+template <typename T> int split_receiver(Scene<T>& s, int32_t sid, int32_t out[4], bool& reshade, int32_t* nbid);
+// isFullPool (shade.cpp:26-30)
+template <typename T> bool pool_full(const Scene<T>& s, int need);
+
 // The threshold method the device uses for cell coordinates, on the host
 // (tests compare it with cell_coord), and the size check run before upload.
 template <typename T> int cell_of_thresholds(const Octree<T>& o, int axis, T q);

@@ -40,8 +40,31 @@ __host__ __device__ inline double int_to_real(int v, double*) {
     double d; std::memcpy(&d, &w, 8); return d;
 #endif
 }
-__device__ __forceinline__ int real_to_int(float f) { return __float_as_int(f); }
-__device__ __forceinline__ int real_to_int(double d) { return (int)__double_as_longlong(d); }
+__host__ __device__ __forceinline__ int real_to_int(float f) {
+#ifdef __CUDA_ARCH__
+    return __float_as_int(f);
+#else
+    int v; std::memcpy(&v, &f, 4); return v;
+#endif
+}
+__host__ __device__ __forceinline__ int real_to_int(double d) {
+#ifdef __CUDA_ARCH__
+    return (int)__double_as_longlong(d);
+#else
+    long long v; std::memcpy(&v, &d, 8); return (int)v;
+#endif
+}
+// read-only load: the non-coherent path on the device, a plain load on the host
+template <typename U>
+__host__ __device__ __forceinline__ U ro_load(const U* p) {
+#ifdef __CUDA_ARCH__
+    return __ldg(p);
+#else
+    return *p;
+#endif
+}
+__host__ __device__ __forceinline__ int imin(int a, int b) { return a < b ? a : b; }
+__host__ __device__ __forceinline__ int imax(int a, int b) { return a > b ? a : b; }
 template <typename T> inline T pack_int(int v) { return int_to_real(v, (T*)nullptr); }
 
 // order-preserving integer image of a key (+0 and -0 equal, as in the
@@ -123,9 +146,9 @@ struct Cnt { unsigned rays, rays_ref, cells, tris, se, prec, capped, loops; };
 // Cell coordinate along one axis: a first guess in T, corrected against the
 // thresholds so the result equals the reference's FP64 expression exactly.
 template <typename T>
-__device__ __forceinline__ int cell_axis(T q, T g0, T inv, const T* th, int D) {
+__host__ __device__ __forceinline__ int cell_axis(T q, T g0, T inv, const T* th, int D) {
     int k = (int)((q - g0) * inv);
-    k = min(max(k, 0), D - 1);
+    k = imin(imax(k, 0), D - 1);
     while (k + 1 < D && q >= th[k + 1]) ++k;
     while (k > 0 && q < th[k]) --k;
     return k;
@@ -148,7 +171,7 @@ __device__ __forceinline__ int cell_axis(T q, T g0, T inv, const T* th, int D) {
 // in `loops`, and the ray is treated as blocked (-3).  A walk the reference
 // finishes never repeats a state, so its result is untouched.
 template <typename T, bool COUNT>
-__device__ __forceinline__ int walk(const Grid<T>& G, const T p[3], const T v[3], int ban, Cnt& c) {
+__host__ __device__ __forceinline__ int walk(const Grid<T>& G, const T p[3], const T v[3], int ban, Cnt& c) {
     T t = 0;
     int prev = -1;
     T q0 = p[0], q1 = p[1], q2 = p[2];
@@ -167,7 +190,7 @@ __device__ __forceinline__ int walk(const Grid<T>& G, const T p[3], const T v[3]
         const int gx = cell_axis(q0, G.g0[0], G.inv_grid, G.thr + G.thr_off[0], G.dims[0]);
         const int gy = cell_axis(q1, G.g0[1], G.inv_grid, G.thr + G.thr_off[1], G.dims[1]);
         const int gz = cell_axis(q2, G.g0[2], G.inv_grid, G.thr + G.thr_off[2], G.dims[2]);
-        const int4 cr = __ldg(&G.cell[(gx * G.dims[1] + gy) * G.dims[2] + gz]);
+        const int4 cr = ro_load(&G.cell[(gx * G.dims[1] + gy) * G.dims[2] + gz]);
         const int leaf = cr.x;
         if (leaf == prev) {          // "Precision Exceeded": step one unit of t
             if (COUNT) c.prec++;
@@ -229,13 +252,13 @@ __device__ __forceinline__ int walk(const Grid<T>& G, const T p[3], const T v[3]
     return -2;
 }
 
-template <typename T> __device__ __forceinline__ T rsqrt_exact(T x);
-template <> __device__ __forceinline__ float rsqrt_exact<float>(float x) { return sqrtf(x); }
-template <> __device__ __forceinline__ double rsqrt_exact<double>(double x) { return sqrt(x); }
+template <typename T> __host__ __device__ __forceinline__ T rsqrt_exact(T x);
+template <> __host__ __device__ __forceinline__ float rsqrt_exact<float>(float x) { return sqrtf(x); }
+template <> __host__ __device__ __forceinline__ double rsqrt_exact<double>(double x) { return sqrt(x); }
 
 // CalFF, shade.cpp:107-127: the pre-test is cheap, the walk is not
 template <typename T, bool COUNT, bool WALK>
-__device__ __forceinline__ T point_ff(const Shooter<T>& s, const Patch<T>& src, const T p[3], const T nd[3], T ndlen,
+__host__ __device__ __forceinline__ T point_ff(const Shooter<T>& s, const Patch<T>& src, const T p[3], const T nd[3], T ndlen,
                                       int logdes, const Grid<T>& G, Cnt& c) {
     const T d[3] = {src.c[0] - p[0], src.c[1] - p[1], src.c[2] - p[2]};
     const T ds = d[0] * s.n[0] + d[1] * s.n[1] + d[2] * s.n[2];
@@ -258,7 +281,7 @@ __device__ __forceinline__ T point_ff(const Shooter<T>& s, const Patch<T>& src, 
 // stray ';' at shade.cpp:164: a split source returns ff(half1)+ff(half2); the
 // whole-source result is discarded, so its walk is not cast.
 template <typename T, bool COUNT>
-__device__ __forceinline__ T corner_ff(const Shooter<T>& s, const T p[3], const T nd[3], T ndlen, int logdes,
+__host__ __device__ __forceinline__ T corner_ff(const Shooter<T>& s, const T p[3], const T nd[3], T ndlen, int logdes,
                                        const Grid<T>& G, Cnt& c) {
     const unsigned before = c.rays;
     if (!s.split) {
@@ -378,22 +401,17 @@ __device__ __forceinline__ void shoot_group(const Slots<T>& S, const Grid<T>& G,
 // Shooter record for slot `slot`: normal, |n|, centre, area, unshot energy,
 // and AdaptCalFF's split into two halves (shade.cpp:76-99, 141-156).
 template <typename T>
-__device__ void build_shooter(const Slots<T>& S, int slot, Shooter<T>& s) {
-    const Q4<T> fr = S.frgb[slot], nn = S.nrm[slot], cc = S.ctr[slot], db = S.deltaB[slot];
-    T p[3][3];
-    for (int v = 0; v < 3; v++) {
-        const Q4<T> q = S.vtx[slot * 3 + v];
-        p[v][0] = q.x; p[v][1] = q.y; p[v][2] = q.z;
-    }
+__host__ __device__ inline void make_shooter(const T p[3][3], const T c[3], const T n[3], T nlen, T area,
+                                             const T deltaB[3], int slot, int logsrc, Shooter<T>& s) {
     s.slot = slot;
-    s.logsrc = (int)fr.w;
+    s.logsrc = logsrc;
     s.pad = 0;
-    s.n[0] = nn.x; s.n[1] = nn.y; s.n[2] = nn.z;
-    s.nlen = nn.w;
-    s.deltaB[0] = db.x; s.deltaB[1] = db.y; s.deltaB[2] = db.z;
+    s.n[0] = n[0]; s.n[1] = n[1]; s.n[2] = n[2];
+    s.nlen = nlen;
+    s.deltaB[0] = deltaB[0]; s.deltaB[1] = deltaB[1]; s.deltaB[2] = deltaB[2];
     s.pad2 = 0;
-    s.part[0].c[0] = cc.x; s.part[0].c[1] = cc.y; s.part[0].c[2] = cc.z;
-    s.part[0].area = cc.w;
+    s.part[0].c[0] = c[0]; s.part[0].c[1] = c[1]; s.part[0].c[2] = c[2];
+    s.part[0].area = area;
     // AdaptCalFF's split decision (shade.cpp:143-156): first longest edge
     int e = 0;
     T longest = 0;
@@ -411,13 +429,25 @@ __device__ void build_shooter(const Slots<T>& S, int slot, Shooter<T>& s) {
             s.part[1].c[q] = (T)((double)(m[q] + p[i2][q] + p[i0][q]) / 3.0);
             s.part[2].c[q] = (T)((double)(m[q] + p[i1][q] + p[i2][q]) / 3.0);
         }
-        s.part[1].area = s.part[2].area = (T)((double)cc.w / 2.0);
+        s.part[1].area = s.part[2].area = (T)((double)area / 2.0);
     } else {
         for (int h = 1; h < 3; h++) {
             for (int q = 0; q < 3; q++) s.part[h].c[q] = 0;
             s.part[h].area = 0;
         }
     }
+}
+
+template <typename T>
+__device__ void build_shooter(const Slots<T>& S, int slot, Shooter<T>& s) {
+    const Q4<T> fr = S.frgb[slot], nn = S.nrm[slot], cc = S.ctr[slot], db = S.deltaB[slot];
+    T p[3][3];
+    for (int v = 0; v < 3; v++) {
+        const Q4<T> q = S.vtx[slot * 3 + v];
+        p[v][0] = q.x; p[v][1] = q.y; p[v][2] = q.z;
+    }
+    const T c[3] = {cc.x, cc.y, cc.z}, n[3] = {nn.x, nn.y, nn.z}, d[3] = {db.x, db.y, db.z};
+    make_shooter(p, c, n, nn.w, cc.w, d, slot, (int)fr.w, s);
 }
 
 

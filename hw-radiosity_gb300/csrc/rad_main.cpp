@@ -59,6 +59,8 @@ void usage(const char* argv0, const rad_options& o) {
     fprintf(stderr, "   GPU Options (extensions)\n");
     fprintf(stderr, "       -device <integer>       CUDA device (default 0)\n");
     fprintf(stderr, "       -fp64                   All-FP64 solver (the reference's float->double build)\n");
+    fprintf(stderr, "       -adaptive               Adaptive split variant (config.h = ADAPT + ROLLBACK: serial\n");
+    fprintf(stderr, "                               loop, delta-FF split test, no pre-partition)\n");
 }
 
 [[noreturn]] void die(const char* what) {
@@ -103,19 +105,67 @@ void write_out(const rad_scene* s, const rad_options& o, const char* prefix, int
     after_write(o, fn);
 }
 
+// DoRadiosity with serialRadiosity (rad.cpp:491-523 without PRE_PARTITION):
+// the adaptive variant updates the host scene in place
+int run_adaptive(rad_scene* scene, rad_octree* tree, const rad_options& o, int device, const char* out, double t2) {
+    rad_adapt* ad = nullptr;
+    check(rad_adapt_create(scene, tree, &o, device, &ad), "device");
+    const int W = o.write_cycle;
+    long long loop = 1;
+    for (;;) {
+        long long target = W > 0 ? ((loop + W - 1) / W) * W : loop + (1LL << 40);
+        int64_t done = 0;
+        int32_t conv = 0;
+        int rc = rad_adapt_run(ad, target - loop + 1, &done, &conv);
+        if (rc == RAD_ERR_WALK) fprintf(stderr, "[" KRED "WARN" KWHT "] %s\n", rad_last_error());
+        else check(rc, "shooting loop");
+        print_log(scene);
+        long long last = loop + done - 1;
+        if (W > 0 && done > 0 && last % W == 0) {
+            fprintf(stderr, "[" KGRN "INFO" KWHT "] Loop %lld BEGIN\n", last);
+            write_out(scene, o, out, (int)last);
+            rad_stats st;
+            rad_adapt_stats(ad, &st, nullptr, nullptr, nullptr);
+            fprintf(stderr, "[" KGRN "INFO" KWHT "] END Loop. There are %i triangles.\n", st.n_slots);
+        }
+        loop = last + 1;
+        if (conv) {
+            if (W > 0 && loop % W == 0) fprintf(stderr, "[" KGRN "INFO" KWHT "] Loop %lld BEGIN\n", loop);
+            break;
+        }
+    }
+    fprintf(stderr, "[" KGRN "INFO" KWHT "] Complete in #Iterations %lld\n", loop);
+    double a = now();
+    write_out(scene, o, out, 0);
+    double b = now();
+    fprintf(stderr, "[" KGRN "INFO" KWHT "] Store file took " KMAG "%f" KWHT " sec. time.\n", b - a);
+    fprintf(stderr, "[" KGRN "INFO" KWHT "] Radiosity Method took " KMAG "%f" KWHT " sec. time.\n", b - t2);
+    rad_stats st;
+    int64_t hp = 0, sp = 0, sm = 0;
+    if (rad_adapt_stats(ad, &st, &hp, &sp, &sm) == RAD_OK)
+        fprintf(stderr, "[" KGRN "GPU" KWHT "] steps %lld, %d triangles, %lld splits, %lld sample points, "
+                "%lld rays (%lld form factors on the host)\n", (long long)st.steps, st.n_slots, (long long)sp,
+                (long long)sm, (long long)st.rays, (long long)hp);
+    rad_adapt_destroy(ad);
+    rad_octree_free(tree);
+    rad_scene_free(scene);
+    return 0;
+}
+
 }  // namespace
 
 int main(int argc, char* argv[]) {
     rad_options o;
     rad_options_default(&o);
     int device = 0;
+    bool adaptive = false;
     if (argc < 3) {
         usage(argv[0], o);
         return 1;
     }
     static const char* opts[] = {"-debug", "-adapt_area", "-sample_area", "-converge", "-delta_ff",
                                  "-write_cycle", "-zip", "-triangle", "-light", "-o", "-interactive",
-                                 "-jobs", "-parallel_src", "-device", "-fp64"};
+                                 "-jobs", "-parallel_src", "-device", "-fp64", "-adaptive"};
     const int n_opts = (int)(sizeof opts / sizeof opts[0]);
     const char* in = nullptr;
     const char* out = "./test";
@@ -146,6 +196,7 @@ int main(int argc, char* argv[]) {
             case 12: geti(o.parallel_src, "Parallel Source Error"); break;
             case 13: geti(device, "Device Error"); break;
             case 14: o.precision = 64; break;
+            case 15: adaptive = true; break;
         }
     }
     fprintf(stderr, "[" KGRN "INFO" KWHT "] Input Model " KMAG "%s" KWHT " and Output Prefix " KMAG "%s\n" KWHT,
@@ -176,6 +227,7 @@ int main(int argc, char* argv[]) {
     double t2 = now();
     check(rad_scene_init(scene), "init");
     print_log(scene);
+    if (adaptive) return run_adaptive(scene, tree, o, device, out, t2);
     check(rad_scene_prepartition(scene), "pre-partition");
     print_log(scene);
     rad_dev* dev = nullptr;

@@ -423,9 +423,11 @@ void bisect(const Slot<T>& s, Slot<T>& t1, Slot<T>& t2, int e) {
 // PartitionTriangleAndStore, shade.cpp:311-431.  out[] receives the slot ids
 // of t1..t4 (-1 where not created).
 template <typename T>
-int split_and_store(Scene<T>& sc, Pool<T>& pool, int32_t sid, int32_t out[4], bool& reshade) {
+int split_and_store(Scene<T>& sc, Pool<T>& pool, int32_t sid, int32_t out[4], bool& reshade,
+                    int32_t* nbid_out = nullptr) {
     reshade = false;
     out[0] = out[1] = out[2] = out[3] = -1;
+    if (nbid_out) *nbid_out = -1;
     if (pool.full(4) || (double)sc.slots[sid].area < 1e-8) return -1;
     int e = 0;
     {
@@ -443,6 +445,7 @@ int split_and_store(Scene<T>& sc, Pool<T>& pool, int32_t sid, int32_t out[4], bo
     }
     int32_t id1 = pool.alloc(), id2 = pool.alloc();
     const int32_t nbid = sc.slots[sid].nb[e];
+    if (nbid_out) *nbid_out = nbid;
     bisect(sc.slots[sid], sc.slots[id1], sc.slots[id2], e);
     int32_t n1, n2;
     sc.slots[id1].nb[1] = n1 = sc.slots[sid].nb[(e + 2) % 3];
@@ -503,6 +506,21 @@ int split_and_store(Scene<T>& sc, Pool<T>& pool, int32_t sid, int32_t out[4], bo
     return replaced;
 }
 }  // namespace
+
+template <typename T>
+int split_receiver(Scene<T>& s, int32_t sid, int32_t out[4], bool& reshade, int32_t* nbid) {
+    Pool<T> pool{s};
+    return split_and_store(s, pool, sid, out, reshade, nbid);
+}
+template int split_receiver<float>(Scene<float>&, int32_t, int32_t*, bool&, int32_t*);
+template int split_receiver<double>(Scene<double>&, int32_t, int32_t*, bool&, int32_t*);
+
+template <typename T>
+bool pool_full(const Scene<T>& s, int need) {
+    return s.trinum + need >= std::min(kMaxTriPool, s.opt.triangle_limit);
+}
+template bool pool_full<float>(const Scene<float>&, int);
+template bool pool_full<double>(const Scene<double>&, int);
 
 template <typename T>
 void prepartition(Scene<T>& s) {

@@ -29,6 +29,7 @@ EXPORTS = [
     "rad_dev_destroy",
     "rad_batch_create", "rad_batch_run", "rad_batch_run_timed", "rad_batch_scene_stats", "rad_batch_download",
     "rad_batch_trace", "rad_batch_stats", "rad_batch_set_counting", "rad_batch_destroy",
+    "rad_adapt_create", "rad_adapt_run", "rad_adapt_trace", "rad_adapt_stats", "rad_adapt_destroy",
 ]
 
 
@@ -116,6 +117,11 @@ def load(path: Optional[str] = None) -> C.CDLL:
         "rad_batch_stats": (C.c_int, [vp, P(Stats)]),
         "rad_batch_set_counting": (C.c_int, [vp, i32]),
         "rad_batch_destroy": (None, [vp]),
+        "rad_adapt_create": (C.c_int, [vp, vp, P(Options), i32, P(vp)]),
+        "rad_adapt_run": (C.c_int, [vp, i64, P(i64), P(i32)]),
+        "rad_adapt_trace": (C.c_int, [vp, vp, i64, P(i64)]),
+        "rad_adapt_stats": (C.c_int, [vp, P(Stats), P(i64), P(i64), P(i64)]),
+        "rad_adapt_destroy": (None, [vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -397,6 +403,47 @@ class Batch:
     def close(self):
         if self.h:
             load().rad_batch_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Adaptive:
+    """Adaptive split variant (``rad_adapt``); updates ``scene`` in place."""
+
+    def __init__(self, scene: Scene, tree: Octree, opts: Options, device: int = 0):
+        self.scene = scene
+        self.h = C.c_void_p()
+        _check(load().rad_adapt_create(scene.h, tree.h, C.byref(opts), device, C.byref(self.h)))
+
+    def run(self, max_steps: int = 1 << 62):
+        sd, cv = C.c_int64(), C.c_int32()
+        rc = _check(load().rad_adapt_run(self.h, max_steps, C.byref(sd), C.byref(cv)), allow=(RAD_ERR_WALK,))
+        return sd.value, bool(cv.value), rc
+
+    def trace(self) -> np.ndarray:
+        n = C.c_int64()
+        _check(load().rad_adapt_trace(self.h, None, 0, C.byref(n)))
+        out = np.zeros(n.value, np.int32)
+        if n.value:
+            _check(load().rad_adapt_trace(self.h, out.ctypes.data, n.value, C.byref(n)))
+        return out.reshape(-1, 1)
+
+    def stats(self) -> Dict[str, int]:
+        s = Stats()
+        hp, sp, sm = C.c_int64(), C.c_int64(), C.c_int64()
+        _check(load().rad_adapt_stats(self.h, C.byref(s), C.byref(hp), C.byref(sp), C.byref(sm)))
+        d = {k: getattr(s, k) for k, _ in Stats._fields_}
+        d.update(host_points=hp.value, splits=sp.value, samples=sm.value)
+        return d
+
+    def close(self):
+        if self.h:
+            load().rad_adapt_destroy(self.h)
             self.h = C.c_void_p()
 
     def __del__(self):

@@ -58,6 +58,7 @@ typedef struct rad_scene rad_scene;   /* host scene store */
 typedef struct rad_octree rad_octree; /* host-built visibility structure */
 typedef struct rad_dev rad_dev;       /* device-resident solver */
 typedef struct rad_batch rad_batch;   /* many independent scenes shot together */
+typedef struct rad_adapt rad_adapt;   /* the adaptive split variant */
 
 /* Read-only view of a scene's live slots (valid until the scene changes or
  * is freed).  Arrays are slot-major; element type float (precision 32) or
@@ -229,6 +230,27 @@ int rad_batch_trace(const rad_batch* b, int32_t scene, int32_t* out, int64_t cap
 int rad_batch_stats(const rad_batch* b, rad_stats* st);
 int rad_batch_set_counting(rad_batch* b, int32_t on);
 void rad_batch_destroy(rad_batch* b);
+
+/* ---- adaptive split variant ---------------------------------------------- */
+
+/* The reference built with include/config.h = ADAPT + ROLLBACK only:
+ * serialRadiosity (rad.cpp:452-490) -- the first strict maximum shoots, and
+ * receivers are visited in slot order -- with the full Shade
+ * (shade.cpp:435-554): receivers of area >= adapt_area whose corner and centre
+ * form factors (and up to area/sample_area rand() sample points) disagree by
+ * more than delta_ff are split along the longest edge, with rollback.  Call
+ * after rad_scene_init and WITHOUT rad_scene_prepartition (that configuration
+ * has none).  The scene is updated in place by rad_adapt_run (topology,
+ * accB, deltaB): write it with rad_scene_write_fin; it must outlive the
+ * handle.  Each step's corner and centre form factors are computed on the
+ * device; the receiver loop, splits and sample points run on the host. */
+int rad_adapt_create(rad_scene* s, const rad_octree* t, const rad_options* o, int32_t device, rad_adapt** out);
+int rad_adapt_run(rad_adapt* a, int64_t max_steps, int64_t* steps_done, int32_t* converged);
+int rad_adapt_trace(const rad_adapt* a, int32_t* out, int64_t cap, int64_t* n);
+/* host_points: form factors evaluated on the host (sample points, receivers
+ * rewritten earlier in their step); splits; rand() sample points drawn. */
+int rad_adapt_stats(const rad_adapt* a, rad_stats* st, int64_t* host_points, int64_t* splits, int64_t* samples);
+void rad_adapt_destroy(rad_adapt* a);
 
 #ifdef __cplusplus
 }
