@@ -216,6 +216,45 @@ def measure_batched(capi, n_scenes, warmup, iters, device):
             "l2": "batch inputs exceed L2; plain timed without flush (graph chunks)"}
 
 
+def measure_adaptive(capi, steps, device, with_reference=True):
+    """The adaptive split variant (ADAPT + ROLLBACK build of the reference) on
+    a 100x100x100 room with 4 boxes that splits from 960 triangles toward the
+    40,000 cap: wall-clock steps/s of the GPU + host solver, next to the
+    reference's own adaptive build (serial by construction) on the same steps."""
+    from hwrad import scenes as S
+    sc_gen = S.room_with_boxes(8, 4, 1, seed=5, size=100.0)
+    argv = sc_gen.argv({"-triangle": "40000", "-converge": "5"})
+    tmp = tempfile.mkdtemp(prefix="radadapt_")
+    tri = sc_gen.write(os.path.join(tmp, "adapt.tri"))
+    o = capi.options_from_argv(argv)
+    sc = capi.Scene.load(tri, o)
+    tree = capi.Octree(sc, _nproc())
+    sc.init()
+    ad = capi.Adaptive(sc, tree, o, device)
+    t0 = time.perf_counter()
+    n, conv, _ = ad.run(steps)
+    dt = time.perf_counter() - t0
+    st = ad.stats()
+    out = {"workload": "room 100^3, 4 boxes, 960 triangles splitting toward the 40,000 cap, -converge 5",
+           "steps": n, "slots_end": st["n_slots"], "steps_per_s": n / dt if dt > 0 else None,
+           "rays": st["rays"], "splits": st["splits"], "host_form_factors": st["host_points"],
+           "sample_points": st["samples"]}
+    ad.close()
+    if with_reference:
+        sys.path.insert(0, os.path.join(REPO, "oracle"))
+        import runner
+        if os.path.exists(runner.REF32A):
+            times = os.path.join(tmp, "times.txt")
+            runner.run(runner.REF32A, tri, argv + ["-jobs", "1"], steps=steps, env={"RAD_TIMES": times},
+                       workdir=tmp, timeout=1800)
+            stamps = [float(x) for x in open(times).read().split()]
+            if len(stamps) > steps:
+                ref = steps / (stamps[steps] - stamps[0])
+                out["reference_steps_per_s"] = ref
+                out["over_reference"] = out["steps_per_s"] / ref if out["steps_per_s"] else None
+    return out
+
+
 def rank_env():
     return (int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0")),
             int(os.environ.get("LOCAL_RANK", "0")))
@@ -291,6 +330,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--batch-scenes", type=int, default=256, help="0 skips the batched measurement")
     ap.add_argument("--batch-iters", type=int, default=100)
+    ap.add_argument("--adaptive-steps", type=int, default=100, help="0 skips the adaptive-variant measurement")
     args = ap.parse_args()
     if os.environ.get("RAD_BENCH_STALL_DUMP"):
         import faulthandler
@@ -412,6 +452,11 @@ def main():
     if args.batch_scenes > 0:
         batched = measure_batched(capi, args.batch_scenes, args.warmup, args.batch_iters, local)
 
+    adaptive = None
+    if args.adaptive_steps > 0:
+        log("adaptive variant")
+        adaptive = measure_adaptive(capi, args.adaptive_steps, local, with_reference=not args.no_cpu_baseline)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         log("cpu baseline")
@@ -443,6 +488,7 @@ def main():
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "note": "rad_dev_create (upload) + run + rad_dev_download over warm-up + timed steps"},
         "batched": batched,
+        "adaptive": adaptive,
         "gpu_launches": done if opts.parallel_src <= 1 else 2 * done,
         "clocks": clocks.summary(),
         "cpu_baseline": cpu,
