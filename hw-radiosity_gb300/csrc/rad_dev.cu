@@ -53,6 +53,21 @@ namespace dev {
 #ifndef RAD_SHOOT_MIN_BLOCKS
 #define RAD_SHOOT_MIN_BLOCKS 3
 #endif
+// a group is split in the next step when its item took longer than this
+// many SM cycles (a split item: the second figure)
+#ifndef RAD_HEAVY_CYCLES
+#define RAD_HEAVY_CYCLES 110000
+#endif
+#ifndef RAD_HEAVY_CYCLES_SPLIT
+#define RAD_HEAVY_CYCLES_SPLIT 55000
+#endif
+// lanes per corner in a heavy group's items, and slots per item
+#ifndef RAD_HEAVY_LANES
+#define RAD_HEAVY_LANES 4
+#endif
+constexpr int kHeavyLanes = RAD_HEAVY_LANES;
+constexpr int kHeavySlots = 32 / (3 * kHeavyLanes);
+constexpr int kHeavyItems = (kSlotsPerWarp + kHeavySlots - 1) / kHeavySlots;   // items per heavy group
 template <typename T, bool COUNT, bool FUSED>
 __global__ void __launch_bounds__(kShootThreads, RAD_SHOOT_MIN_BLOCKS)
 k_shoot(Slots<T> S, Grid<T> G, Shooter<T>* shooters, State* st, Partial* __restrict__ part, T conv) {
@@ -80,12 +95,38 @@ k_shoot(Slots<T> S, Grid<T> G, Shooter<T>* shooters, State* st, Partial* __restr
     unsigned long long kk = 0;
     int ks = -1;
     Cnt c = {0, 0, 0, 0, 0, 0, 0, 0};
+    // the queue: the heavy groups' one-slot items first, then the other groups
+    const bool split = !COUNT && FUSED && st->heavy_on;
+    const int s = (int)st->steps;
+    const int n_heavy_items = split ? st->heavy_n[s & 1] * kHeavyItems : 0;
     for (;;) {
         int g = 0;
         if (lane == 0) g = atomicAdd(&st->work, 1);
         g = __shfl_sync(kFull, g, 0);
-        if (g >= n_groups) break;
-        shoot_group<T, COUNT>(S, Gs, sh, nsh, g, lane, conv, kk, ks, c);
+        int grp;
+        const long long t_item = clock64();
+        if constexpr (!COUNT) {
+            if (g < n_heavy_items) {
+                grp = st->heavy[(s & 1) * n_groups + g / kHeavyItems];
+                const int part = (g % kHeavyItems) * kHeavySlots;
+                shoot_item<T, false, kHeavyLanes>(S, Gs, sh, nsh, grp * kSlotsPerWarp + part,
+                                                  imin(kHeavySlots, kSlotsPerWarp - part), lane, conv, kk, ks, c);
+            }
+        }
+        if (g >= n_heavy_items) {
+            grp = g - n_heavy_items;
+            if (grp >= n_groups) break;
+            if (split && __ldcg(&st->stamp[grp]) >= s) continue;   // its items are in the heavy part
+            shoot_group<T, COUNT>(S, Gs, sh, nsh, grp, lane, conv, kk, ks, c);
+        }
+        if (split && lane == 0) {
+            const long long dt = clock64() - t_item;
+            if (dt > (g < n_heavy_items ? st->heavy_cycles_split : st->heavy_cycles) &&
+                atomicMax(&st->stamp[grp], s + 1) < s + 1) {
+                const int q = atomicAdd(&st->heavy_n[(s + 1) & 1], 1);
+                st->heavy[((s + 1) & 1) * n_groups + q] = grp;
+            }
+        }
     }
     warp_max(kk, ks);
     flush_counters<COUNT>(st, c, lane);
@@ -137,6 +178,7 @@ k_shoot(Slots<T> S, Grid<T> G, Shooter<T>* shooters, State* st, Partial* __restr
         st->steps = steps;
         st->work = 0;
         st->ctas_done = 0;
+        st->heavy_n[(steps + 1) & 1] = 0;   // consumed by this step, refilled by the next
     }
 }
 
@@ -423,15 +465,24 @@ int upload(const Scene<T>& s, const Octree<T>& o, const rad_options& opt, int de
         const int want = (n_groups + kShootThreads / 32 - 1) / (kShootThreads / 32);
         d.n_cta = std::max(1, std::min(want, std::max(1, sms * per_sm)));
     }
+    const int n_groups = (n + kSlotsPerWarp - 1) / kSlotsPerWarp;
+    int *d_heavy, *d_stamp;
     if ((rc = d.alloc(&d.d_shooters, (size_t)d.P)) || (rc = d.alloc(&d.d_state, 1)) ||
-        (rc = d.alloc(&d.d_part, (size_t)d.n_cta)))
+        (rc = d.alloc(&d.d_part, (size_t)d.n_cta)) || (rc = d.alloc(&d_heavy, 2 * (size_t)n_groups)) ||
+        (rc = d.alloc(&d_stamp, (size_t)n_groups)))
         return rc;
+    CU(cudaMemsetAsync(d_stamp, 0xff, (size_t)n_groups * sizeof(int), d.stream));
     d.trace_cap = 1 << 16;
     CU(cudaMalloc(&d.d_trace, (size_t)d.trace_cap * 4));
     State st{};
     st.step_limit = 0;
     st.trace = d.d_trace;
     st.trace_cap = d.trace_cap;
+    st.heavy = d_heavy;
+    st.stamp = d_stamp;
+    st.heavy_on = d.P == 1;
+    st.heavy_cycles = RAD_HEAVY_CYCLES;
+    st.heavy_cycles_split = RAD_HEAVY_CYCLES_SPLIT;
     CU(cudaMemcpyAsync(d.d_state, &st, sizeof st, cudaMemcpyHostToDevice, d.stream));
     CU(cudaMemsetAsync(d.d_shooters, 0, sizeof(Shooter<T>) * d.P, d.stream));
     CU(cudaMemsetAsync(d.d_part, 0, sizeof(Partial) * d.n_cta, d.stream));

@@ -128,7 +128,7 @@ __host__ __device__ inline size_t kMaxShooterBytes(int nsh) {
 }
 
 struct State {
-    int work;               // next 10-slot group of the current step (k_shoot queue)
+    int work;               // next work item of the current step (k_shoot queue)
     int ctas_done;          // CTAs of the current k_shoot that have finished (fused selection)
     int done;               // a selection found no candidate
     int paused;             // step limit reached
@@ -139,6 +139,16 @@ struct State {
     long long trace_cap;
     int* trace;
     unsigned long long rays, rays_ref, cells, tris, se, prec, capped, loops;
+    // Groups whose item took longer than heavy_cycles (split items:
+    // heavy_cycles_split) in step s are listed in heavy[(s+1)&1] and stamped
+    // s+1; step s+1 hands each out first, as items of a few slots whose
+    // corners are cast by several lanes each.  Only the schedule depends on
+    // it, not the results.
+    int* heavy;             // 2 x n_groups
+    int* stamp;             // per group: the last step it was split in (-1: never)
+    int heavy_n[2];
+    int heavy_on;           // one shooter per step (the fused kernel)
+    long long heavy_cycles, heavy_cycles_split;
 };
 
 struct Cnt { unsigned rays, rays_ref, cells, tris, se, prec, capped, loops; };
@@ -155,6 +165,74 @@ __host__ __device__ __forceinline__ int cell_axis(T q, T g0, T inv, const T* th,
 }
 
 // ------------------------------------------------------------------ walk
+// TreeNodeNum (raycast.cpp:254-281) as a table lookup: the cell record
+// (leaf, list begin, list end, 0) of the cell holding q; the cell coordinate
+// (int)(((double)q - G0) / MinGridLen) per axis is found exactly from the
+// thresholds.
+template <typename T>
+__host__ __device__ __forceinline__ int4 cell_at(const Grid<T>& G, T q0, T q1, T q2) {
+    const int gx = cell_axis(q0, G.g0[0], G.inv_grid, G.thr + G.thr_off[0], G.dims[0]);
+    const int gy = cell_axis(q1, G.g0[1], G.inv_grid, G.thr + G.thr_off[1], G.dims[1]);
+    const int gz = cell_axis(q2, G.g0[2], G.inv_grid, G.thr + G.thr_off[2], G.dims[2]);
+    return ro_load(&G.cell[(gx * G.dims[1] + gy) * G.dims[2] + gz]);
+}
+
+// NextPoint (raycast.cpp:235-251): leave the leaf box [lo, hi] measured from
+// the ray origin, overshoot by 0.1 in t; returns the new t.
+template <typename T>
+__host__ __device__ __forceinline__ T next_t(const Grid<T>& G, const T p[3], const T v[3], const Q4<T>& lo,
+                                             const Q4<T>& hi) {
+    const T bl[3] = {lo.x, lo.y, lo.z}, bh[3] = {hi.x, hi.y, hi.z};
+    T tm = (T)1000000.0;
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        if (fabs(v[a]) > G.v_eps) {             // fabs((double)v) > 1e-6
+            const T s = (v[a] > 0) ? (bh[a] - p[a]) / v[a] : (bl[a] - p[a]) / v[a];
+            tm = (s < tm) ? s : tm;
+        }
+    }
+    return (T)((double)tm + 0.1);
+}
+
+// TriListHitted/TriHitted (raycast.cpp:283-333) over entries [b, e) of one
+// leaf's list: the nearest hit of the list (first one on ties), or -1.
+template <typename T, bool COUNT>
+__host__ __device__ __forceinline__ int scan_list(const Grid<T>& G, const T p[3], const T v[3], int ban, int b, int e,
+                                                  Cnt& c) {
+    T tmin = (T)1000000.0;
+    int best = -1;
+    // the next entry's (n, id) and (c) records are in flight while this one is tested
+    Q4<T> nx_en = {0, 0, 0, 0}, nx_ec = {0, 0, 0, 0};
+    if (b < e) { nx_en = G.entry[5 * b]; nx_ec = G.entry[5 * b + 1]; }
+    for (int k = b; k < e; ++k) {
+        const Q4<T> en = nx_en, ec = nx_ec;
+        if (k + 1 < e) { nx_en = G.entry[5 * (k + 1)]; nx_ec = G.entry[5 * (k + 1) + 1]; }
+        const int id = real_to_int(en.w);
+        if (id == ban) continue;
+        if (COUNT) c.tris++;
+        const T a1 = v[0] * en.x + v[1] * en.y + v[2] * en.z;
+        const T w0 = ec.x - p[0], w1 = ec.y - p[1], w2 = ec.z - p[2];
+        const T a2 = w0 * en.x + w1 * en.y + w2 * en.z;
+        // a2/a1 is negative or zero when the signs differ or a2 is zero
+        // (a1 nonzero): the test below rejects it, so skip the division
+        if ((a1 > 0 && a2 <= 0) || (a1 < 0 && a2 >= 0)) continue;
+        const T tt = a2 / a1;
+        if (tt < G.t_eps) continue;            // (double)t < 0.0001
+        if (tt >= tmin) continue;
+        if (COUNT) c.se++;
+        const T x = p[0] + tt * v[0], y = p[1] + tt * v[1], z = p[2] + tt * v[2];
+        const Q4<T> s0 = G.entry[5 * k + 2];
+        if ((x * s0.x + y * s0.y + z * s0.z + s0.w) < 0.0) continue;
+        const Q4<T> s1 = G.entry[5 * k + 3];
+        if ((x * s1.x + y * s1.y + z * s1.z + s1.w) < 0.0) continue;
+        const Q4<T> s2 = G.entry[5 * k + 4];
+        if ((x * s2.x + y * s2.y + z * s2.z + s2.w) < 0.0) continue;
+        tmin = tt;
+        best = id;
+    }
+    return best;
+}
+
 // RayHitted (raycast.cpp:335-360) with TreeNodeNum (254-281) as a table
 // lookup, TriListHitted/TriHitted (283-333) and NextPoint (235-251).
 //
@@ -186,11 +264,7 @@ __host__ __device__ __forceinline__ int walk(const Grid<T>& G, const T p[3], con
         }
         if (++lam == power) { chk_t = t; chk_prev = prev; power <<= 1; lam = 0; }
         if (COUNT) c.cells++;
-        // (int)(((double)q - G0) / MinGridLen) per axis, found exactly from the thresholds
-        const int gx = cell_axis(q0, G.g0[0], G.inv_grid, G.thr + G.thr_off[0], G.dims[0]);
-        const int gy = cell_axis(q1, G.g0[1], G.inv_grid, G.thr + G.thr_off[1], G.dims[1]);
-        const int gz = cell_axis(q2, G.g0[2], G.inv_grid, G.thr + G.thr_off[2], G.dims[2]);
-        const int4 cr = ro_load(&G.cell[(gx * G.dims[1] + gy) * G.dims[2] + gz]);
+        const int4 cr = cell_at(G, q0, q1, q2);
         const int leaf = cr.x;
         if (leaf == prev) {          // "Precision Exceeded": step one unit of t
             if (COUNT) c.prec++;
@@ -200,28 +274,68 @@ __host__ __device__ __forceinline__ int walk(const Grid<T>& G, const T p[3], con
         }
         // the leaf box (needed after the list) and the list itself load in parallel
         const Q4<T> lo = G.leaf[2 * leaf], hi = G.leaf[2 * leaf + 1];
+        const int best = scan_list<T, COUNT>(G, p, v, ban, cr.y, cr.z, c);
+        if (best >= 0) return best;
+        prev = leaf;
+        t = next_t(G, p, v, lo, hi);
+        q0 = p[0] + t * v[0]; q1 = p[1] + t * v[1]; q2 = p[2] + t * v[2];
+    }
+    c.capped++;
+    return -2;
+}
+
+#ifdef __CUDACC__
+// The same walk cast by a group of L lanes (L a power of two, the group's
+// lanes in `gmask`, this lane's index in it `sub`).  All L lanes step through
+// the cells together; lane `sub` scans entries b+sub, b+sub+L, ... of each
+// list with the serial scan's running minimum, and the group then takes the
+// smallest (tt, entry index).  The serial scan keeps the first entry with the
+// smallest valid tt, so without a NaN the results are equal.  A 0/0 plane
+// test (ray in the triangle's plane) makes tt NaN, which the serial scan
+// folds in its own way: a list that produces one is scanned serially.
+// Ray and cycle counters are kept by lane 0 of the group only.
+template <typename T, int L>
+__device__ __forceinline__ int walk_lanes(const Grid<T>& G, const T p[3], const T v[3], int ban, int sub,
+                                          unsigned gmask, Cnt& c) {
+    T t = 0;
+    int prev = -1;
+    T q0 = p[0], q1 = p[1], q2 = p[2];
+    T chk_t = (T)-1;
+    int chk_prev = -2, power = 1, lam = 0;
+    for (int it = 0; it < G.walk_cap; ++it) {
+        if (q0 < G.g0[0] || q0 > G.g1[0] || q1 < G.g0[1] || q1 > G.g1[1] || q2 < G.g0[2] || q2 > G.g1[2])
+            return -1;
+        if (t == chk_t && prev == chk_prev) {
+            if (sub == 0) c.loops++;
+            return -3;
+        }
+        if (++lam == power) { chk_t = t; chk_prev = prev; power <<= 1; lam = 0; }
+        const int4 cr = cell_at(G, q0, q1, q2);
+        const int leaf = cr.x;
+        if (leaf == prev) {          // "Precision Exceeded": step one unit of t
+            t = (T)((double)t + 1.0);
+            q0 = p[0] + t * v[0]; q1 = p[1] + t * v[1]; q2 = p[2] + t * v[2];
+            continue;
+        }
+        const Q4<T> lo = G.leaf[2 * leaf], hi = G.leaf[2 * leaf + 1];
         const int b = cr.y, e = cr.z;
         T tmin = (T)1000000.0;
-        int best = -1;
-        // the next entry's (n, id) and (c) records are in flight while this one is tested
+        int bk = -1;
+        bool nan = false;
         Q4<T> nx_en = {0, 0, 0, 0}, nx_ec = {0, 0, 0, 0};
-        if (b < e) { nx_en = G.entry[5 * b]; nx_ec = G.entry[5 * b + 1]; }
-        for (int k = b; k < e; ++k) {
+        if (b + sub < e) { nx_en = G.entry[5 * (b + sub)]; nx_ec = G.entry[5 * (b + sub) + 1]; }
+        for (int k = b + sub; k < e; k += L) {
             const Q4<T> en = nx_en, ec = nx_ec;
-            if (k + 1 < e) { nx_en = G.entry[5 * (k + 1)]; nx_ec = G.entry[5 * (k + 1) + 1]; }
-            const int id = real_to_int(en.w);
-            if (id == ban) continue;
-            if (COUNT) c.tris++;
+            if (k + L < e) { nx_en = G.entry[5 * (k + L)]; nx_ec = G.entry[5 * (k + L) + 1]; }
+            if (real_to_int(en.w) == ban) continue;
             const T a1 = v[0] * en.x + v[1] * en.y + v[2] * en.z;
             const T w0 = ec.x - p[0], w1 = ec.y - p[1], w2 = ec.z - p[2];
             const T a2 = w0 * en.x + w1 * en.y + w2 * en.z;
-            // a2/a1 is negative or zero when the signs differ or a2 is zero
-            // (a1 nonzero): the test below rejects it, so skip the division
             if ((a1 > 0 && a2 <= 0) || (a1 < 0 && a2 >= 0)) continue;
             const T tt = a2 / a1;
-            if (tt < G.t_eps) continue;            // (double)t < 0.0001
+            if (tt != tt) { nan = true; continue; }
+            if (tt < G.t_eps) continue;
             if (tt >= tmin) continue;
-            if (COUNT) c.se++;
             const T x = p[0] + tt * v[0], y = p[1] + tt * v[1], z = p[2] + tt * v[2];
             const Q4<T> s0 = G.entry[5 * k + 2];
             if ((x * s0.x + y * s0.y + z * s0.z + s0.w) < 0.0) continue;
@@ -230,52 +344,65 @@ __host__ __device__ __forceinline__ int walk(const Grid<T>& G, const T p[3], con
             const Q4<T> s2 = G.entry[5 * k + 4];
             if ((x * s2.x + y * s2.y + z * s2.z + s2.w) < 0.0) continue;
             tmin = tt;
-            best = id;
+            bk = k;
         }
-        if (best >= 0) return best;
-        prev = leaf;
-        // NextPoint: leave the cell from the ray origin, overshoot by 0.1 in t
-        const T bl[3] = {lo.x, lo.y, lo.z}, bh[3] = {hi.x, hi.y, hi.z};
-        T tm = (T)1000000.0;
 #pragma unroll
-        for (int a = 0; a < 3; a++) {
-            if (fabs(v[a]) > G.v_eps) {             // fabs((double)v) > 1e-6
-                const T s = (v[a] > 0) ? (bh[a] - p[a]) / v[a] : (bl[a] - p[a]) / v[a];
-                tm = (s < tm) ? s : tm;
-            }
+        for (int d = 1; d < L; d <<= 1) {
+            const T ot = __shfl_xor_sync(gmask, tmin, d);
+            const int ok = __shfl_xor_sync(gmask, bk, d);
+            if (ok >= 0 && (bk < 0 || ot < tmin || (ot == tmin && ok < bk))) { tmin = ot; bk = ok; }
         }
-        tm = (T)((double)tm + 0.1);
-        q0 = p[0] + tm * v[0]; q1 = p[1] + tm * v[1]; q2 = p[2] + tm * v[2];
-        t = tm;
+        int hit = -1;
+        if (__any_sync(gmask, nan))
+            hit = scan_list<T, false>(G, p, v, ban, b, e, c);
+        else if (bk >= 0)
+            hit = real_to_int(G.entry[5 * bk].w);
+        if (hit >= 0) return hit;
+        prev = leaf;
+        t = next_t(G, p, v, lo, hi);
+        q0 = p[0] + t * v[0]; q1 = p[1] + t * v[1]; q2 = p[2] + t * v[2];
     }
-    c.capped++;
+    if (sub == 0) c.capped++;
     return -2;
 }
+#endif
+
 
 template <typename T> __host__ __device__ __forceinline__ T rsqrt_exact(T x);
 template <> __host__ __device__ __forceinline__ float rsqrt_exact<float>(float x) { return sqrtf(x); }
 template <> __host__ __device__ __forceinline__ double rsqrt_exact<double>(double x) { return sqrt(x); }
 
-// CalFF, shade.cpp:107-127: the pre-test is cheap, the walk is not
-template <typename T, bool COUNT, bool WALK>
-__host__ __device__ __forceinline__ T point_ff(const Shooter<T>& s, const Patch<T>& src, const T p[3], const T nd[3], T ndlen,
-                                      int logdes, const Grid<T>& G, Cnt& c) {
-    const T d[3] = {src.c[0] - p[0], src.c[1] - p[1], src.c[2] - p[2]};
+// CalFF's unoccluded part, shade.cpp:107-124: false when the pre-test
+// rejects the pair (ff 0, no ray); else ff and the ray direction d.
+template <typename T>
+__host__ __device__ __forceinline__ bool point_pre(const Shooter<T>& s, const Patch<T>& src, const T p[3], const T nd[3],
+                                                   T ndlen, T d[3], T& ff) {
+    d[0] = src.c[0] - p[0]; d[1] = src.c[1] - p[1]; d[2] = src.c[2] - p[2];
     const T ds = d[0] * s.n[0] + d[1] * s.n[1] + d[2] * s.n[2];
     const T dd = -(d[0] * nd[0] + d[1] * nd[1] + d[2] * nd[2]);
-    if ((ds < 0) != (dd < 0)) return 0;
+    if ((ds < 0) != (dd < 0)) return false;
     const T d2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
     const T dl = rsqrt_exact<T>(d2);
     const T c1 = ds / dl / s.nlen;
     const T c2 = dd / dl / ndlen;
-    T ff = c1 * c2;
-    if (ff <= 0.0) return 0;
+    ff = c1 * c2;
+    if (ff <= 0.0) return false;
     ff = (T)((double)ff * ((double)src.area / ((double)d2 * kPiD)));
-    if (ff <= 0.0) return 0;
+    if (ff <= 0.0) return false;
+    return true;
+}
+
+// CalFF, shade.cpp:107-127: the pre-test is cheap, the walk is not
+template <typename T, bool COUNT, bool WALK>
+__host__ __device__ __forceinline__ T point_ff(const Shooter<T>& s, const Patch<T>& src, const T p[3], const T nd[3], T ndlen,
+                                      int logdes, const Grid<T>& G, Cnt& c) {
+    T d[3], ff = 0;
+    if (!point_pre(s, src, p, nd, ndlen, d, ff)) return 0;
     if (!WALK) return ff;   // pre-test only (reference ray accounting)
     c.rays++;
     return walk<T, COUNT>(G, p, d, logdes, c) == s.logsrc ? ff : (T)0;
 }
+
 
 // Shade's per-corner AdaptCalFF(CalFF(...)), shade.cpp:442-450 with the
 // stray ';' at shade.cpp:164: a split source returns ff(half1)+ff(half2); the
@@ -295,6 +422,27 @@ __host__ __device__ __forceinline__ T corner_ff(const Shooter<T>& s, const T p[3
     if (COUNT) c.rays_ref += c.rays - before;
     return f1 + f2;
 }
+
+#ifdef __CUDACC__
+// point_ff / corner_ff (no counting) for a group of L lanes sharing one corner
+template <typename T, int L>
+__device__ __forceinline__ T point_ff_lanes(const Shooter<T>& s, const Patch<T>& src, const T p[3], const T nd[3],
+                                            T ndlen, int logdes, int sub, unsigned gmask, const Grid<T>& G, Cnt& c) {
+    T d[3], ff = 0;
+    if (!point_pre(s, src, p, nd, ndlen, d, ff)) return 0;
+    if (sub == 0) c.rays++;
+    return walk_lanes<T, L>(G, p, d, logdes, sub, gmask, c) == s.logsrc ? ff : (T)0;
+}
+
+template <typename T, int L>
+__device__ __forceinline__ T corner_ff_lanes(const Shooter<T>& s, const T p[3], const T nd[3], T ndlen, int logdes,
+                                             int sub, unsigned gmask, const Grid<T>& G, Cnt& c) {
+    if (!s.split) return point_ff_lanes<T, L>(s, s.part[0], p, nd, ndlen, logdes, sub, gmask, G, c);
+    const T f1 = point_ff_lanes<T, L>(s, s.part[1], p, nd, ndlen, logdes, sub, gmask, G, c);
+    const T f2 = point_ff_lanes<T, L>(s, s.part[2], p, nd, ndlen, logdes, sub, gmask, G, c);
+    return f1 + f2;
+}
+#endif
 
 template <typename T>
 __device__ __forceinline__ T shfl(T v, int src) { return __shfl_sync(kFull, v, src); }
@@ -326,13 +474,24 @@ __device__ __forceinline__ void flush_counters(State* st, Cnt& c, int lane) {
 }
 
 // ------------------------------------------------------------------ k_shoot
-// One 10-slot group: lanes 3r+v are corner v of slot g*10+r.
-template <typename T, bool COUNT>
-__device__ __forceinline__ void shoot_group(const Slots<T>& S, const Grid<T>& G, const Shooter<T>* sh, int nsh,
-                                            int g, int lane, T conv, unsigned long long& kk, int& ks, Cnt& c) {
-    const int r = lane / 3, v = lane - 3 * r;
-    const int i = g * kSlotsPerWarp + r;
-    const bool own = lane < 3 * kSlotsPerWarp && i < S.n;
+// One work item: n_item consecutive slots from slot i0, each corner's ray cast
+// by a group of L lanes.  Lane = L*(3r+v) + sub: corner v of slot i0+r, lane
+// `sub` of its group.  L = 1 is the common layout (10 slots, one lane per
+// corner); L = 4 serves two slots of a group whose walks were long in the
+// previous step.
+// The deposit is the same for every layout: the three corners' form factors
+// meet by shuffle, the group's lane 0 writes its corner's accB, and corner 0's
+// lane 0 keeps the slot's deltaB in the reference's order.
+template <typename T, bool COUNT, int L>
+__device__ __forceinline__ void shoot_item(const Slots<T>& S, const Grid<T>& G, const Shooter<T>* sh, int nsh, int i0,
+                                           int n_item, int lane, T conv, unsigned long long& kk, int& ks, Cnt& c) {
+    static_assert(L == 1 || !COUNT, "the counting pass uses the serial walk");
+    const int ray = lane / L, sub = lane - L * ray;
+    const int r = ray / 3, v = ray - 3 * r;
+    const int i = i0 + r;
+    const bool own = ray < 3 * n_item && i < S.n;
+    const unsigned gmask = L == 1 ? 1u << lane : (L == 32 ? kFull : ((1u << L) - 1u) << (lane & ~(L - 1)));
+    const bool lead = sub == 0;
 
     Q4<T> fr = {0, 0, 0, (T)-1}, acc = {0, 0, 0, 0}, db = {0, 0, 0, 0};
     if (own) {
@@ -346,8 +505,8 @@ __device__ __forceinline__ void shoot_group(const Slots<T>& S, const Grid<T>& G,
     // a receiver is skipped only when all nine accB components are >= 255
     const bool open_v = live && (acc.x < (T)255 || acc.y < (T)255 || acc.z < (T)255);
     const unsigned ballot = __ballot_sync(kFull, open_v);
-    const int base = 3 * min(r, kSlotsPerWarp - 1);
-    const bool open = ((ballot >> base) & 7u) != 0;
+    const int base = 3 * L * min(r, n_item - 1);   // lane 0 of corner 0 of slot r
+    const bool open = (((ballot >> base) | (ballot >> (base + L)) | (ballot >> (base + 2 * L))) & 1u) != 0;
     const bool active = live && !is_src && open && nsh > 0;
     if (live && v == 0) db = S.deltaB[i];
 
@@ -364,8 +523,13 @@ __device__ __forceinline__ void shoot_group(const Slots<T>& S, const Grid<T>& G,
     T d0 = db.x, d1 = db.y, d2 = db.z;
     for (int j = 0; j < nsh; j++) {
         T ff = 0;
-        if (active) ff = corner_ff<T, COUNT>(sh[j], pv, nd, ndlen, parent, G, c);
-        const T f0 = shfl(ff, base), f1 = shfl(ff, base + 1), f2 = shfl(ff, base + 2);
+        if (active) {
+            if constexpr (L == 1)
+                ff = corner_ff<T, COUNT>(sh[j], pv, nd, ndlen, parent, G, c);
+            else
+                ff = corner_ff_lanes<T, L>(sh[j], pv, nd, ndlen, parent, sub, gmask, G, c);
+        }
+        const T f0 = shfl(ff, base), f1 = shfl(ff, base + L), f2 = shfl(ff, base + 2 * L);
         if (active) {
             const T lo0 = fr.x * k * sh[j].deltaB[0] / 3;
             const T lo1 = fr.y * k * sh[j].deltaB[1] / 3;
@@ -378,24 +542,30 @@ __device__ __forceinline__ void shoot_group(const Slots<T>& S, const Grid<T>& G,
             }
         }
     }
-    if (active) {
+    if (active && lead) {
         Q4<T> o = {a0, a1, a2, acc.w};
         S.accB[i * 3 + v] = o;
         if (v == 0) { Q4<T> q = {d0, d1, d2, db.w}; S.deltaB[i] = q; }
     }
     if (live && is_src && v == 0) {       // rad.cpp:446-449
         d0 = d1 = d2 = 0;
-        Q4<T> q = {0, 0, 0, db.w};
-        S.deltaB[i] = q;
+        if (lead) { Q4<T> q = {0, 0, 0, db.w}; S.deltaB[i] = q; }
     }
     // next selection: key = (dB0 + dB1) + dB2 (rad.cpp:394), candidates > converge
-    if (live && v == 0) {
+    if (live && v == 0 && lead) {
         const T key = (d0 + d1) + d2;
         if (key > conv) {
             const unsigned long long o = key_order(key);
             if (part_less(kk, ks, o, i)) { kk = o; ks = i; }
         }
     }
+}
+
+// One 10-slot group in the common layout (lanes 3r+v: corner v of slot g*10+r).
+template <typename T, bool COUNT>
+__device__ __forceinline__ void shoot_group(const Slots<T>& S, const Grid<T>& G, const Shooter<T>* sh, int nsh,
+                                            int g, int lane, T conv, unsigned long long& kk, int& ks, Cnt& c) {
+    shoot_item<T, COUNT, 1>(S, G, sh, nsh, g * kSlotsPerWarp, kSlotsPerWarp, lane, conv, kk, ks, c);
 }
 
 // Shooter record for slot `slot`: normal, |n|, centre, area, unshot energy,
