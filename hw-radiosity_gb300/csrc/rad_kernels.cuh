@@ -7,6 +7,7 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <type_traits>
 #include <vector>
 
 #include "rad_host.h"
@@ -76,6 +77,92 @@ __device__ __forceinline__ unsigned long long key_order(float f) {
 __device__ __forceinline__ unsigned long long key_order(double f) {
     unsigned long long u = (unsigned long long)__double_as_longlong(f == 0.0 ? 0.0 : f);
     return (u >> 63) ? ~u : (u | 0x8000000000000000ull);
+}
+
+// ------------------------------------------------------------------ FP64-free forms
+// The reference promotes two hot expressions to double: the walk's overshoot
+// (float)((double)t + 0.1) and CalFF's scale (float)((double)ff * ((double)a /
+// ((double)d2 * PI))).  FP64 is slow on this GPU (a float->double add->float
+// chain measured 191 cycles, a double multiply+divide 642), so both have FP32
+// forms that are exact where they answer and fall back to the double
+// expression near a float rounding boundary.  Exhaustive and random checks
+// against the double expressions are in tests/test_host.py.
+__host__ __device__ __forceinline__ unsigned f2u(float f) {
+#ifdef __CUDA_ARCH__
+    return __float_as_uint(f);
+#else
+    unsigned u;
+    std::memcpy(&u, &f, 4);
+    return u;
+#endif
+}
+__host__ __device__ __forceinline__ float u2f(unsigned u) {
+#ifdef __CUDA_ARCH__
+    return __uint_as_float(u);
+#else
+    float f;
+    std::memcpy(&f, &u, 4);
+    return f;
+#endif
+}
+
+// (float)((double)x + 0.1).  With c = 0.1 (double), s = x + 0.1f rounded and
+// e its exact error (TwoSum), the exact sum is s + T, T = e + (c - 0.1f).  For
+// s >= 1/16, T lies within one float step of s (|c - 0.1f| = 1.49e-9 is below
+// half the spacing under s), so the answer is s or a neighbour, chosen by
+// comparing T with the half-spacings above and below s.  Rounding c + x to
+// double first moves the sum by at most 2^-30 of the spacing; T is known to
+// 2^-24 of it; answers within 2^-18 of a spacing of a midpoint are left to the
+// double expression.
+__host__ __device__ __forceinline__ float add_tenth(float x) {
+    const float c_hi = 0x1.99999ap-4f;          // 0.1f
+    const float c_lo = -0x1.99999ap-30f;        // 0.1 - 0.1f, rounded to float
+    const float s = x + c_hi;
+    const float bv = s - x;
+    const float av = s - bv;
+    const float e = (x - av) + (c_hi - bv);     // s + e == x + 0.1f exactly
+    if (s >= 0.0625f && s < 0x1p100f) {
+        const float t = e + c_lo;
+        const unsigned bits = f2u(s);
+        const float up = u2f((bits & 0x7f800000u) - (23u << 23));   // spacing above s
+        const float dn = (bits & 0x007fffffu) ? up : up * 0.5f;     // spacing below s
+        const float h_up = up * 0.5f, h_dn = dn * 0.5f, m = up * 0x1p-18f;
+        if (fabsf(t - h_up) > m && fabsf(t + h_dn) > m) {
+            if (t > h_up) return u2f(bits + 1);
+            if (t < -h_dn) return u2f(bits - 1);
+            return s;
+        }
+    }
+    return (float)((double)x + 0.1);
+}
+
+// (float)((double)f * ((double)a / ((double)d2 * pi))), pi the double constant:
+// f*a / (d2*pi) in float-float arithmetic (product errors by fma, pi as a
+// float pair, one correction of the quotient), relative error below 2^-42.
+// The double expression differs from the exact value by at most 3 * 2^-53, so
+// when the float-float value is more than 2^-14 of a float spacing from every
+// rounding midpoint both round to the same float.
+__host__ __device__ __forceinline__ float ff_scale(float f, float a, float d2) {
+    const float pi_hi = 0x1.921fb6p+1f, pi_lo = -0x1.777a5cp-24f;
+    const float den_hi = d2 * pi_hi;
+    const float den_lo = fmaf(d2, pi_hi, -den_hi) + d2 * pi_lo;
+    const float num_hi = f * a;
+    const float num_lo = fmaf(f, a, -num_hi);
+    const float q1 = num_hi / den_hi;
+    if (num_hi >= 0x1p-90f && num_hi <= 0x1p90f && den_hi >= 0x1p-90f && den_hi <= 0x1p90f && q1 >= 0x1p-90f &&
+        q1 <= 0x1p90f) {
+        const float r = (fmaf(-q1, den_hi, num_hi) + num_lo) - q1 * den_lo;
+        const float q2 = r / den_hi;
+        const float y = q1 + q2;
+        const float bv = y - q1;
+        const float z = (q1 - (y - bv)) + (q2 - bv);   // y + z == q1 + q2 exactly
+        const unsigned bits = f2u(y);
+        const float up = u2f((bits & 0x7f800000u) - (23u << 23));
+        const float dn = (bits & 0x007fffffu) ? up : up * 0.5f;
+        const float m = up * 0x1p-14f;
+        if (z < up * 0.5f - m && z > -dn * 0.5f + m) return y;
+    }
+    return (float)((double)f * ((double)a / ((double)d2 * kPiD)));
 }
 
 // Visibility structure (kernel parameter; constant for a handle).
@@ -191,7 +278,10 @@ __host__ __device__ __forceinline__ T next_t(const Grid<T>& G, const T p[3], con
             tm = (s < tm) ? s : tm;
         }
     }
-    return (T)((double)tm + 0.1);
+    if constexpr (std::is_same<T, float>::value)
+        return add_tenth(tm);
+    else
+        return tm + 0.1;
 }
 
 // TriListHitted/TriHitted (raycast.cpp:283-333) over entries [b, e) of one
@@ -387,7 +477,10 @@ __host__ __device__ __forceinline__ bool point_pre(const Shooter<T>& s, const Pa
     const T c2 = dd / dl / ndlen;
     ff = c1 * c2;
     if (ff <= 0.0) return false;
-    ff = (T)((double)ff * ((double)src.area / ((double)d2 * kPiD)));
+    if constexpr (std::is_same<T, float>::value)
+        ff = ff_scale(ff, src.area, d2);
+    else
+        ff = (T)((double)ff * ((double)src.area / ((double)d2 * kPiD)));
     if (ff <= 0.0) return false;
     return true;
 }

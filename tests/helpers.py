@@ -47,3 +47,19 @@ def rel_l2(a, b):
     b = np.asarray(b, np.float64).ravel()
     den = np.linalg.norm(b)
     return float(np.linalg.norm(a - b) / den) if den > 0 else float(np.linalg.norm(a - b))
+
+
+def build_fp_forms_check(workdir):
+    """Compile tests/fp_forms_check.cu (host and device checks of the FP32
+    forms of the reference's double expressions) with the solver's flags."""
+    import shutil
+    import subprocess
+    here = os.path.dirname(os.path.abspath(__file__))
+    repo = os.path.dirname(here)
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    exe = os.path.join(workdir, "fp_forms_check")
+    subprocess.run([nvcc, "-gencode", "arch=compute_103a,code=sm_103a", "-O2", "-std=c++17", "-fmad=false",
+                    "--prec-div=true", "--prec-sqrt=true", "-Xcompiler", "-ffp-contract=off,-O2",
+                    "-I", os.path.join(repo, "hw-radiosity_gb300", "csrc"), "-I", os.path.join(repo, "include"),
+                    "-o", exe, os.path.join(here, "fp_forms_check.cu")], check=True, capture_output=True)
+    return exe

@@ -70,3 +70,14 @@ def test_precision_stress(built, workdir):
         with open(out, "w") as fh:
             json.dump(report, fh, indent=1)
     print(json.dumps(report))
+
+
+def test_fp32_forms_on_device(workdir):
+    """The same FP32 forms compiled for the device (IEEE division, no
+    contraction) against the double expressions on the device: 200 M inputs."""
+    import subprocess
+    from helpers import build_fp_forms_check
+    exe = build_fp_forms_check(workdir)
+    r = subprocess.run([exe, "gpu", "200000000"], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert r.stdout.split() == ["ok", "200000000"]

@@ -163,3 +163,17 @@ def test_rand_restatement_equals_libc(built, workdir):
     subprocess.run(["gcc", "-O2", "-std=c11", "-o", exe, src, "-lm"], check=True, capture_output=True)
     got = [int(x) for x in subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split()]
     assert got == want
+
+
+def test_fp32_forms_equal_double_expressions(workdir):
+    """The walk's overshoot (float)((double)t + 0.1) and CalFF's scale
+    (float)((double)ff * ((double)a / ((double)d2 * PI))) have FP32 forms
+    (add_tenth, ff_scale) that fall back to the double expression only near
+    a rounding midpoint.  add_tenth: every float bit pattern; ff_scale: 20 M
+    triples, one in eight placed next to a rounding midpoint."""
+    import subprocess
+    from helpers import build_fp_forms_check
+    exe = build_fp_forms_check(workdir)
+    r = subprocess.run([exe, "cpu", "1", "20000000"], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert r.stdout.split() == ["ok", str(1 << 32), "20000000"]
