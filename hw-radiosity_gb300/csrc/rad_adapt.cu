@@ -223,7 +223,6 @@ int adapt_create(Scene<T>& s, const Octree<T>& o, const rad_options& opt, int de
     a.Gh = grid_params(o, opt.walk_cap);
     a.Gh.thr = a.pack.thr.data();
     a.Gh.cell = a.pack.cell.data();
-    a.Gh.leaf = a.pack.leaf.data();
     a.Gh.entry = a.pack.ent.data();
     a.cap = (int)s.slots.size();
     int rc;
@@ -233,16 +232,15 @@ int adapt_create(Scene<T>& s, const Octree<T>& o, const rad_options& opt, int de
         CU(cudaMemcpyAsync(*dst, src.data(), src.size() * sizeof(src[0]), cudaMemcpyHostToDevice, a.stream));
         return RAD_OK;
     };
-    Q4<T> *d_leaf, *d_ent;
-    int4* d_cell;
+    Q4<T>* d_ent;
+    CellRec<T>* d_cell;
     T* d_thr;
-    if ((rc = put(&d_leaf, a.pack.leaf)) || (rc = put(&d_ent, a.pack.ent)) || (rc = put(&d_cell, a.pack.cell)) ||
+    if ((rc = put(&d_ent, a.pack.ent)) || (rc = put(&d_cell, a.pack.cell)) ||
         (rc = put(&d_thr, a.pack.thr)))
         return rc;
     a.Gd = a.Gh;
     a.Gd.thr = d_thr;
     a.Gd.cell = d_cell;
-    a.Gd.leaf = d_leaf;
     a.Gd.entry = d_ent;
     if ((rc = a.alloc(&a.d_vtx, (size_t)a.cap * 3)) || (rc = a.alloc(&a.d_nrm, (size_t)a.cap)) ||
         (rc = a.alloc(&a.d_ctr, (size_t)a.cap)) || (rc = a.alloc(&a.d_frgb, (size_t)a.cap)) ||

@@ -307,8 +307,8 @@ int rad_batch_create(const rad_scene* const* scenes, const rad_octree* const* tr
     }
     if (total_groups > 0x7fffffffLL || (long long)trace_cap * n_scenes > 0x7fffffffLL)
         return bail(fail(RAD_ERR_CAPACITY, "batch too large"));
-    Q4<float> *d_vtx, *d_nrm, *d_ctr, *d_frgb, *d_acc, *d_db, *d_leaf, *d_ent;
-    int4* d_cell;
+    Q4<float> *d_vtx, *d_nrm, *d_ctr, *d_frgb, *d_acc, *d_db, *d_ent;
+    CellRec<float>* d_cell;
     float* d_thr;
     int rc;
     auto put = [&](auto** dst, const auto& src) -> int {
@@ -319,7 +319,7 @@ int rad_batch_create(const rad_scene* const* scenes, const rad_octree* const* tr
     };
     if ((rc = put(&d_vtx, P.vtx)) || (rc = put(&d_nrm, P.nrm)) || (rc = put(&d_ctr, P.ctr)) ||
         (rc = put(&d_frgb, P.frgb)) || (rc = put(&d_acc, P.acc)) || (rc = put(&d_db, P.db)) ||
-        (rc = put(&d_leaf, P.leaf)) || (rc = put(&d_ent, P.ent)) || (rc = put(&d_cell, P.cell)) ||
+        (rc = put(&d_ent, P.ent)) || (rc = put(&d_cell, P.cell)) ||
         (rc = put(&d_thr, P.thr)))
         return bail(rc);
     b->desc.resize(n_scenes);
@@ -331,7 +331,6 @@ int rad_batch_create(const rad_scene* const* scenes, const rad_octree* const* tr
         d.G = grid_params(trees[s]->o32, opts[s].walk_cap);
         d.G.thr = d_thr + o.thr;
         d.G.cell = d_cell + o.cell;
-        d.G.leaf = d_leaf + o.leaf * 2;
         d.G.entry = d_ent + o.ent * 5;
         d.conv = opts[s].converge;
         d.trace_off = s * trace_cap;

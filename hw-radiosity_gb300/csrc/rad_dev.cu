@@ -426,8 +426,8 @@ int upload(const Scene<T>& s, const Octree<T>& o, const rad_options& opt, int de
     if (!thresholds_consistent(o)) return fail(RAD_ERR_ARG, "octree cell thresholds do not match its dimensions");
     HostPack<T> P;
     pack_scene(s, o, P);
-    Q4<T> *d_vtx, *d_nrm, *d_ctr, *d_frgb, *d_acc, *d_db, *d_leaf, *d_ent;
-    int4* d_cell;
+    Q4<T> *d_vtx, *d_nrm, *d_ctr, *d_frgb, *d_acc, *d_db, *d_ent;
+    CellRec<T>* d_cell;
     T* d_thr;
     int rc;
     auto put = [&](auto** dst, const auto& src) -> int {
@@ -438,14 +438,13 @@ int upload(const Scene<T>& s, const Octree<T>& o, const rad_options& opt, int de
     };
     if ((rc = put(&d_vtx, P.vtx)) || (rc = put(&d_nrm, P.nrm)) || (rc = put(&d_ctr, P.ctr)) ||
         (rc = put(&d_frgb, P.frgb)) || (rc = put(&d_acc, P.acc)) || (rc = put(&d_db, P.db)) ||
-        (rc = put(&d_leaf, P.leaf)) || (rc = put(&d_ent, P.ent)) || (rc = put(&d_cell, P.cell)) ||
+        (rc = put(&d_ent, P.ent)) || (rc = put(&d_cell, P.cell)) ||
         (rc = put(&d_thr, P.thr)))
         return rc;
     d.S = Slots<T>{n, d_vtx, d_nrm, d_ctr, d_frgb, d_acc, d_db};
     Grid<T> G = grid_params(o, opt.walk_cap);
     G.thr = d_thr;
     G.cell = d_cell;
-    G.leaf = d_leaf;
     G.entry = d_ent;
     d.G = G;
 

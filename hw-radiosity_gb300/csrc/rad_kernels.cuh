@@ -165,6 +165,15 @@ __host__ __device__ __forceinline__ float ff_scale(float f, float a, float d2) {
     return (float)((double)f * ((double)a / ((double)d2 * kPiD)));
 }
 
+// One cell of the dense cell table: the leaf holding it (TreeNodeNum), that
+// leaf's triangle-list range and box, so one 48-byte read (FP32) gives the
+// walk everything it needs for the cell.
+template <typename T>
+struct CellRec {
+    int4 h;        // (leaf, list begin, list end, 0)
+    Q4<T> a, b;    // (lo.x, lo.y, lo.z, hi.x) (hi.y, hi.z, 0, 0)
+};
+
 // Visibility structure (kernel parameter; constant for a handle).
 template <typename T>
 struct Grid {
@@ -175,8 +184,7 @@ struct Grid {
     int thr_off[3];
     int n_thr;
     const T* thr;                            // cell-coordinate thresholds (global; staged to smem)
-    const int4* __restrict__ cell;           // cell coordinate triple -> (leaf, list begin, list end, 0)
-    const Q4<T>* __restrict__ leaf;          // 2 per leaf: (g0, begin) (g1, end)
+    const CellRec<T>* __restrict__ cell;     // cell coordinate triple -> leaf, list range, leaf box
     const Q4<T>* __restrict__ entry;         // 5 per list entry: (n, id) (c, 0) se0 se1 se2
     int walk_cap;
 };
@@ -252,16 +260,30 @@ __host__ __device__ __forceinline__ int cell_axis(T q, T g0, T inv, const T* th,
 }
 
 // ------------------------------------------------------------------ walk
-// TreeNodeNum (raycast.cpp:254-281) as a table lookup: the cell record
-// (leaf, list begin, list end, 0) of the cell holding q; the cell coordinate
-// (int)(((double)q - G0) / MinGridLen) per axis is found exactly from the
-// thresholds.
 template <typename T>
-__host__ __device__ __forceinline__ int4 cell_at(const Grid<T>& G, T q0, T q1, T q2) {
+struct Cell {
+    int leaf, b, e;    // leaf, list [b, e)
+    Q4<T> lo, hi;      // leaf box
+};
+
+// TreeNodeNum (raycast.cpp:254-281) as a table lookup: the cell holding q;
+// the cell coordinate (int)(((double)q - G0) / MinGridLen) per axis is found
+// exactly from the thresholds.  The record's three parts load together.
+template <typename T>
+__host__ __device__ __forceinline__ Cell<T> cell_at(const Grid<T>& G, T q0, T q1, T q2) {
     const int gx = cell_axis(q0, G.g0[0], G.inv_grid, G.thr + G.thr_off[0], G.dims[0]);
     const int gy = cell_axis(q1, G.g0[1], G.inv_grid, G.thr + G.thr_off[1], G.dims[1]);
     const int gz = cell_axis(q2, G.g0[2], G.inv_grid, G.thr + G.thr_off[2], G.dims[2]);
-    return ro_load(&G.cell[(gx * G.dims[1] + gy) * G.dims[2] + gz]);
+    const CellRec<T>* r = &G.cell[(gx * G.dims[1] + gy) * G.dims[2] + gz];
+    const int4 h = ro_load(&r->h);
+    const Q4<T> a = r->a, b = r->b;
+    Cell<T> out;
+    out.leaf = h.x;
+    out.b = h.y;
+    out.e = h.z;
+    out.lo = {a.x, a.y, a.z, 0};
+    out.hi = {a.w, b.x, b.y, 0};
+    return out;
 }
 
 // NextPoint (raycast.cpp:235-251): leave the leaf box [lo, hi] measured from
@@ -354,20 +376,18 @@ __host__ __device__ __forceinline__ int walk(const Grid<T>& G, const T p[3], con
         }
         if (++lam == power) { chk_t = t; chk_prev = prev; power <<= 1; lam = 0; }
         if (COUNT) c.cells++;
-        const int4 cr = cell_at(G, q0, q1, q2);
-        const int leaf = cr.x;
+        const Cell<T> cr = cell_at(G, q0, q1, q2);
+        const int leaf = cr.leaf;
         if (leaf == prev) {          // "Precision Exceeded": step one unit of t
             if (COUNT) c.prec++;
             t = (T)((double)t + 1.0);
             q0 = p[0] + t * v[0]; q1 = p[1] + t * v[1]; q2 = p[2] + t * v[2];
             continue;
         }
-        // the leaf box (needed after the list) and the list itself load in parallel
-        const Q4<T> lo = G.leaf[2 * leaf], hi = G.leaf[2 * leaf + 1];
-        const int best = scan_list<T, COUNT>(G, p, v, ban, cr.y, cr.z, c);
+        const int best = scan_list<T, COUNT>(G, p, v, ban, cr.b, cr.e, c);
         if (best >= 0) return best;
         prev = leaf;
-        t = next_t(G, p, v, lo, hi);
+        t = next_t(G, p, v, cr.lo, cr.hi);
         q0 = p[0] + t * v[0]; q1 = p[1] + t * v[1]; q2 = p[2] + t * v[2];
     }
     c.capped++;
@@ -400,15 +420,14 @@ __device__ __forceinline__ int walk_lanes(const Grid<T>& G, const T p[3], const 
             return -3;
         }
         if (++lam == power) { chk_t = t; chk_prev = prev; power <<= 1; lam = 0; }
-        const int4 cr = cell_at(G, q0, q1, q2);
-        const int leaf = cr.x;
+        const Cell<T> cr = cell_at(G, q0, q1, q2);
+        const int leaf = cr.leaf;
         if (leaf == prev) {          // "Precision Exceeded": step one unit of t
             t = (T)((double)t + 1.0);
             q0 = p[0] + t * v[0]; q1 = p[1] + t * v[1]; q2 = p[2] + t * v[2];
             continue;
         }
-        const Q4<T> lo = G.leaf[2 * leaf], hi = G.leaf[2 * leaf + 1];
-        const int b = cr.y, e = cr.z;
+        const int b = cr.b, e = cr.e;
         T tmin = (T)1000000.0;
         int bk = -1;
         bool nan = false;
@@ -449,7 +468,7 @@ __device__ __forceinline__ int walk_lanes(const Grid<T>& G, const T p[3], const 
             hit = real_to_int(G.entry[5 * bk].w);
         if (hit >= 0) return hit;
         prev = leaf;
-        t = next_t(G, p, v, lo, hi);
+        t = next_t(G, p, v, cr.lo, cr.hi);
         q0 = p[0] + t * v[0]; q1 = p[1] + t * v[1]; q2 = p[2] + t * v[2];
     }
     if (sub == 0) c.capped++;
@@ -721,13 +740,13 @@ __device__ void build_shooter(const Slots<T>& S, int slot, Shooter<T>& s) {
 // as RayHitted reads TriStore at shooting time.
 template <typename T>
 struct HostPack {
-    std::vector<Q4<T>> vtx, nrm, ctr, frgb, acc, db, leaf, ent;
-    std::vector<int4> cell;
+    std::vector<Q4<T>> vtx, nrm, ctr, frgb, acc, db, ent;
+    std::vector<CellRec<T>> cell;
     std::vector<T> thr;
 };
 
 struct PackOffsets {
-    size_t slot = 0, leaf = 0, ent = 0, cell = 0, thr = 0;
+    size_t slot = 0, ent = 0, cell = 0, thr = 0;
     int n = 0;
 };
 
@@ -735,7 +754,6 @@ template <typename T>
 inline PackOffsets pack_scene(const Scene<T>& s, const Octree<T>& o, HostPack<T>& P) {
     PackOffsets off;
     off.slot = P.frgb.size();
-    off.leaf = P.leaf.size() / 2;
     off.ent = P.ent.size() / 5;
     off.cell = P.cell.size();
     off.thr = P.thr.size();
@@ -752,12 +770,6 @@ inline PackOffsets pack_scene(const Scene<T>& s, const Octree<T>& o, HostPack<T>
         P.frgb.push_back({(T)t.Frgb[0], (T)t.Frgb[1], (T)t.Frgb[2], (T)t.parent});
         P.db.push_back({t.deltaB[0], t.deltaB[1], t.deltaB[2], 0});
     }
-    const int n_leaves = (int)(o.leaf_range.size() / 2);
-    for (int l = 0; l < n_leaves; l++) {
-        const T* b = &o.leaf_box[(size_t)l * 8];
-        P.leaf.push_back({b[0], b[1], b[2], pack_int<T>(o.leaf_range[2 * l])});
-        P.leaf.push_back({b[4], b[5], b[6], pack_int<T>(o.leaf_range[2 * l + 1])});
-    }
     for (size_t k = 0; k < o.entry_tri.size(); k++) {
         const int id = o.entry_tri[k];
         const Slot<T>& t = s.slots[id];
@@ -765,7 +777,14 @@ inline PackOffsets pack_scene(const Scene<T>& s, const Octree<T>& o, HostPack<T>
         P.ent.push_back({t.c[0], t.c[1], t.c[2], 0});
         for (int e = 0; e < 3; e++) P.ent.push_back({t.se[e][0], t.se[e][1], t.se[e][2], t.se[e][3]});
     }
-    for (int32_t l : o.cell_leaf) P.cell.push_back(make_int4(l, o.leaf_range[2 * l], o.leaf_range[2 * l + 1], 0));
+    for (int32_t l : o.cell_leaf) {
+        const T* b = &o.leaf_box[(size_t)l * 8];
+        CellRec<T> r;
+        r.h = make_int4(l, o.leaf_range[2 * l], o.leaf_range[2 * l + 1], 0);
+        r.a = {b[0], b[1], b[2], b[4]};
+        r.b = {b[5], b[6], 0, 0};
+        P.cell.push_back(r);
+    }
     P.thr.insert(P.thr.end(), o.thr.begin(), o.thr.end());
     return off;
 }
