@@ -5,7 +5,9 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <algorithm>
 #include <string>
+#include <vector>
 
 #include "rad_gb300.h"
 
@@ -61,6 +63,12 @@ void usage(const char* argv0, const rad_options& o) {
     fprintf(stderr, "       -fp64                   All-FP64 solver (the reference's float->double build)\n");
     fprintf(stderr, "       -adaptive               Adaptive split variant (config.h = ADAPT + ROLLBACK: serial\n");
     fprintf(stderr, "                               loop, delta-FF split test, no pre-partition)\n");
+    fprintf(stderr, "   Headless render of the result (the WebGL viewer's initial view, CUDA rasteriser)\n");
+    fprintf(stderr, "       -render <file.ppm>      Write the final result as the viewer shows it\n");
+    fprintf(stderr, "       -render_gouraud         Gouraud shading (default: flat, the viewer's default)\n");
+    fprintf(stderr, "       -render_size <w> <h>    Image size (default 1024 768, the viewer's canvas)\n");
+    fprintf(stderr, "       -render_rot <x> <y>     Rotation about x then y, degrees (default 0 0)\n");
+    fprintf(stderr, "   %s -render_fin <in.fin> <out.ppm> [render options]   render an existing result\n", argv0);
 }
 
 [[noreturn]] void die(const char* what) {
@@ -94,6 +102,55 @@ void after_write(const rad_options& o, const std::string& fn) {
         int ret = system(cmd.c_str());
         fprintf(stderr, "WebGL: %s, return %d\n", cmd.c_str(), ret);
     }
+}
+
+// headless render of the final result (-render)
+const char* g_render = nullptr;
+rad_render_options g_ro;
+
+void write_ppm(const char* path, const std::vector<uint8_t>& rgba, int w, int h) {
+    FILE* f = fopen(path, "wb");
+    if (!f) {
+        fprintf(stderr, "[" KRED "ERR" KWHT "] cannot write %s\n", path);
+        exit(1);
+    }
+    fprintf(f, "P6\n%d %d\n255\n", w, h);
+    std::vector<uint8_t> rgb((size_t)w * h * 3);
+    for (size_t i = 0; i < (size_t)w * h; i++)
+        for (int c = 0; c < 3; c++) rgb[i * 3 + c] = rgba[i * 4 + c];
+    fwrite(rgb.data(), 1, rgb.size(), f);
+    fclose(f);
+}
+
+void render_out(const rad_scene* s, int device) {
+    if (!g_render) return;
+    std::vector<uint8_t> img((size_t)g_ro.width * g_ro.height * 4);
+    check(rad_render_scene(s, &g_ro, device, img.data()), "render");
+    write_ppm(g_render, img, g_ro.width, g_ro.height);
+    fprintf(stderr, "[" KGRN "INFO" KWHT "] Rendered %dx%d image " KMAG "%s\n" KWHT, g_ro.width, g_ro.height, g_render);
+}
+
+// render options shared by -render and -render_fin; returns the number of arguments used, 0 if none
+int render_opt(int argc, char** argv, int i) {
+    auto num = [&](int k, const char* what) -> const char* {
+        if (i + k >= argc) die(what);
+        return argv[i + k];
+    };
+    if (!strcmp(argv[i], "-render_gouraud")) { g_ro.shading = 1; return 1; }
+    if (!strcmp(argv[i], "-render_size")) {
+        if (sscanf(num(1, "RenderSize Error"), "%d", &g_ro.width) != 1 ||
+            sscanf(num(2, "RenderSize Error"), "%d", &g_ro.height) != 1)
+            die("RenderSize Error");
+        return 3;
+    }
+    if (!strcmp(argv[i], "-render_rot")) {
+        if (sscanf(num(1, "RenderRot Error"), "%f", &g_ro.x_rot) != 1 ||
+            sscanf(num(2, "RenderRot Error"), "%f", &g_ro.y_rot) != 1)
+            die("RenderRot Error");
+        return 3;
+    }
+    if (!strcmp(argv[i], "-render")) { g_render = num(1, "Render path missing"); return 2; }
+    return 0;
 }
 
 void write_out(const rad_scene* s, const rad_options& o, const char* prefix, int loop) {
@@ -140,6 +197,7 @@ int run_adaptive(rad_scene* scene, rad_octree* tree, const rad_options& o, int d
     double b = now();
     fprintf(stderr, "[" KGRN "INFO" KWHT "] Store file took " KMAG "%f" KWHT " sec. time.\n", b - a);
     fprintf(stderr, "[" KGRN "INFO" KWHT "] Radiosity Method took " KMAG "%f" KWHT " sec. time.\n", b - t2);
+    render_out(scene, device);
     rad_stats st;
     int64_t hp = 0, sp = 0, sm = 0;
     if (rad_adapt_stats(ad, &st, &hp, &sp, &sm) == RAD_OK)
@@ -157,11 +215,31 @@ int run_adaptive(rad_scene* scene, rad_octree* tree, const rad_options& o, int d
 int main(int argc, char* argv[]) {
     rad_options o;
     rad_options_default(&o);
+    rad_render_options_default(&g_ro);
     int device = 0;
     bool adaptive = false;
     if (argc < 3) {
         usage(argv[0], o);
         return 1;
+    }
+    if (!strcmp(argv[1], "-render_fin")) {   // render an existing .fin, no solve
+        if (argc < 4) {
+            usage(argv[0], o);
+            return 1;
+        }
+        for (int i = 4; i < argc;) {
+            int k = render_opt(argc, argv, i);
+            if (!k && !strcmp(argv[i], "-device") && i + 1 < argc) {
+                device = atoi(argv[i + 1]);
+                k = 2;
+            }
+            if (!k) die("unknown render option");
+            i += k;
+        }
+        std::vector<uint8_t> img((size_t)std::max(g_ro.width, 1) * std::max(g_ro.height, 1) * 4);
+        check(rad_render_fin(argv[2], &g_ro, device, img.data()), "render");
+        write_ppm(argv[3], img, g_ro.width, g_ro.height);
+        return 0;
     }
     static const char* opts[] = {"-debug", "-adapt_area", "-sample_area", "-converge", "-delta_ff",
                                  "-write_cycle", "-zip", "-triangle", "-light", "-o", "-interactive",
@@ -170,6 +248,10 @@ int main(int argc, char* argv[]) {
     const char* in = nullptr;
     const char* out = "./test";
     for (int i = 1; i < argc; i++) {
+        if (int k = render_opt(argc, argv, i)) {
+            i += k - 1;
+            continue;
+        }
         int j = 0;
         for (; j < n_opts; j++)
             if (!strcmp(argv[i], opts[j])) break;
@@ -267,6 +349,7 @@ int main(int argc, char* argv[]) {
         double b = now();
         fprintf(stderr, "[" KGRN "INFO" KWHT "] Store file took " KMAG "%f" KWHT " sec. time.\n", b - a);
     }
+    render_out(scene, device);
     double t3 = now();
     fprintf(stderr, "[" KGRN "INFO" KWHT "] Radiosity Method took " KMAG "%f" KWHT " sec. time.\n", t3 - t2);
     rad_stats st;

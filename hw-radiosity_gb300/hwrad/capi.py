@@ -30,6 +30,7 @@ EXPORTS = [
     "rad_batch_create", "rad_batch_run", "rad_batch_run_timed", "rad_batch_scene_stats", "rad_batch_download",
     "rad_batch_trace", "rad_batch_stats", "rad_batch_set_counting", "rad_batch_destroy",
     "rad_adapt_create", "rad_adapt_run", "rad_adapt_trace", "rad_adapt_stats", "rad_adapt_destroy",
+    "rad_render_options_default", "rad_render_fin", "rad_render_scene",
 ]
 
 
@@ -122,6 +123,9 @@ def load(path: Optional[str] = None) -> C.CDLL:
         "rad_adapt_trace": (C.c_int, [vp, vp, i64, P(i64)]),
         "rad_adapt_stats": (C.c_int, [vp, P(Stats), P(i64), P(i64), P(i64)]),
         "rad_adapt_destroy": (None, [vp]),
+        "rad_render_options_default": (None, [P(RenderOptions)]),
+        "rad_render_fin": (C.c_int, [C.c_char_p, P(RenderOptions), i32, vp]),
+        "rad_render_scene": (C.c_int, [vp, P(RenderOptions), i32, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -451,6 +455,42 @@ class Adaptive:
             self.close()
         except Exception:
             pass
+
+
+class RenderOptions(C.Structure):
+    """rad_render_options: the headless viewer's canvas, shading and rotation."""
+    _fields_ = [("width", C.c_int32), ("height", C.c_int32), ("shading", C.c_int32), ("pad", C.c_int32),
+                ("x_rot", C.c_float), ("y_rot", C.c_float)]
+
+
+def render_options(width=None, height=None, shading="flat", x_rot=0.0, y_rot=0.0) -> RenderOptions:
+    o = RenderOptions()
+    load().rad_render_options_default(C.byref(o))
+    if width is not None:
+        o.width = int(width)
+    if height is not None:
+        o.height = int(height)
+    o.shading = {"flat": 0, "gouraud": 1}[shading]
+    o.x_rot = float(x_rot)
+    o.y_rot = float(y_rot)
+    return o
+
+
+def _render(call, arg, o: RenderOptions, device: int):
+    import numpy as np
+    img = np.empty((o.height, o.width, 4), dtype=np.uint8)
+    _check(call(arg, C.byref(o), device, img.ctypes.data))
+    return img
+
+
+def render_fin(path: str, device: int = 0, **kw):
+    """RGBA8 image (height, width, 4), top row first, of a .fin result as the viewer shows it."""
+    return _render(load().rad_render_fin, path.encode(), render_options(**kw), device)
+
+
+def render_scene(scene: "Scene", device: int = 0, **kw):
+    """The same image of a scene in memory (the triangles its .fin would hold)."""
+    return _render(load().rad_render_scene, scene.h, render_options(**kw), device)
 
 
 def solve(tri_path: str, opts: Options, device: int = 0, max_steps: int = 1 << 62):

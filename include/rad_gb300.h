@@ -252,6 +252,27 @@ int rad_adapt_trace(const rad_adapt* a, int32_t* out, int64_t cap, int64_t* n);
 int rad_adapt_stats(const rad_adapt* a, rad_stats* st, int64_t* host_points, int64_t* splits, int64_t* samples);
 void rad_adapt_destroy(rad_adapt* a);
 
+/* ---------------------------------------------------------------- headless render
+ * Replaces the reference's WebGL viewer path for a result: the model
+ * converter (WebGL_demo/model-converter/main.cpp:167-246, JSON writer 81-150)
+ * and the viewer's shaders in their initial state (WebGL_demo/public/index.html
+ * drawScene 354-380, defaults 555-600; lib/flat.vs, flat.fs, gouraud.vs,
+ * gouraud.fs), rasterised by CUDA kernels into an RGBA8 buffer, top row first.
+ * No graphics API is used.  The reference has no C entry point for this; the
+ * viewer runs in a browser on the converter's JSON. */
+typedef struct rad_render_options {
+    int32_t width, height;   /* pixels; default 1024 x 768 (the viewer's canvas), at most 16384 each */
+    int32_t shading;         /* 0 flat (the viewer's default), 1 gouraud */
+    int32_t pad;
+    float x_rot, y_rot;      /* degrees, the viewer's eyeview.xRot / yRot; default 0 */
+} rad_render_options;
+
+void rad_render_options_default(rad_render_options* o);
+/* render a .fin file (the reference's or ours); rgba holds width*height*4 bytes */
+int rad_render_fin(const char* fin_path, const rad_render_options* o, int32_t device, uint8_t* rgba);
+/* render a scene in memory: the triangles its .fin would hold */
+int rad_render_scene(const rad_scene* s, const rad_render_options* o, int32_t device, uint8_t* rgba);
+
 #ifdef __cplusplus
 }
 #endif

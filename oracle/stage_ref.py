@@ -167,6 +167,12 @@ def main():
             os.makedirs(os.path.dirname(p), exist_ok=True)
             with open(p, "w") as f:
                 f.write(text)
+    # the result viewer's model converter (one file, unpatched): pins the
+    # converter half of the headless renderer's input preparation
+    conv = os.path.join(args.ref, "WebGL_demo", "model-converter", "main.cpp")
+    if os.path.exists(conv):
+        os.makedirs(os.path.join(args.out, "src_conv"), exist_ok=True)
+        shutil.copyfile(conv, os.path.join(args.out, "src_conv", "main.cpp"))
     print(f"stage_ref: staged patched reference into {args.out}/src and src64")
     return 0
 
