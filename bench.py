@@ -255,6 +255,39 @@ def measure_adaptive(capi, steps, device, with_reference=True):
     return out
 
 
+def measure_render(capi, scene, device, reps, with_oracle=True):
+    """Headless render of the config-2 result as the viewer shows it (1024x768,
+    flat and Gouraud): end-to-end images/s of rad_render_scene and of
+    rad_render_fin (converter restatement on the host, upload, CUDA raster,
+    download), next to the C++ restatement (oracle/raster_oracle, one core)
+    on the same .fin."""
+    tmp = tempfile.mkdtemp(prefix="radrender_")
+    prefix = os.path.join(tmp, "result")
+    scene.write_fin(prefix)
+    fin = prefix + ".fin"
+    out = {"workload": "config-2 result, 1024x768, the viewer's initial view", "reps": reps}
+    for shading in ("flat", "gouraud"):
+        capi.render_scene(scene, device, shading=shading)     # warm-up
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            capi.render_scene(scene, device, shading=shading)
+        out[f"{shading}_scene_images_per_s"] = reps / (time.perf_counter() - t0)
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            capi.render_fin(fin, device, shading=shading)
+        out[f"{shading}_fin_images_per_s"] = reps / (time.perf_counter() - t0)
+        if with_oracle:
+            sys.path.insert(0, os.path.join(REPO, "oracle"))
+            import runner
+            exe = os.path.join(runner.HERE, "_build", "raster_oracle")
+            if os.path.exists(exe):
+                t0 = time.perf_counter()
+                subprocess.run([exe, fin, os.path.join(tmp, "o.rgba"), "1024", "768",
+                                "0" if shading == "flat" else "1", "0", "0"], check=True)
+                out[f"{shading}_restatement_cpu_images_per_s"] = 1.0 / (time.perf_counter() - t0)
+    return out
+
+
 def rank_env():
     return (int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0")),
             int(os.environ.get("LOCAL_RANK", "0")))
@@ -331,6 +364,7 @@ def main():
     ap.add_argument("--batch-scenes", type=int, default=256, help="0 skips the batched measurement")
     ap.add_argument("--batch-iters", type=int, default=100)
     ap.add_argument("--adaptive-steps", type=int, default=100, help="0 skips the adaptive-variant measurement")
+    ap.add_argument("--render-reps", type=int, default=5, help="0 skips the headless-render measurement")
     args = ap.parse_args()
     if os.environ.get("RAD_BENCH_STALL_DUMP"):
         import faulthandler
@@ -457,6 +491,11 @@ def main():
         log("adaptive variant")
         adaptive = measure_adaptive(capi, args.adaptive_steps, local, with_reference=not args.no_cpu_baseline)
 
+    render = None
+    if args.render_reps > 0 and rank == 0:
+        log("headless render")
+        render = measure_render(capi, scene, local, args.render_reps, with_oracle=not args.no_cpu_baseline)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         log("cpu baseline")
@@ -489,6 +528,7 @@ def main():
                 "note": "rad_dev_create (upload) + run + rad_dev_download over warm-up + timed steps"},
         "batched": batched,
         "adaptive": adaptive,
+        "render": render,
         "gpu_launches": done if opts.parallel_src <= 1 else 2 * done,
         "clocks": clocks.summary(),
         "cpu_baseline": cpu,

@@ -55,24 +55,32 @@ struct Mesh {
     int n = 0;
 };
 
-static bool read_line(FILE* f, std::string& line) {
-    line.clear();
-    int c;
-    while ((c = std::fgetc(f)) != EOF) {
-        if (c == '\n') return true;
-        line.push_back((char)c);
+// the next line of a text held in memory (without its '\n'), as getline
+struct Lines {
+    const char* p;
+    const char* end;
+    bool next(const char*& b, const char*& e) {
+        if (p >= end) return false;
+        b = p;
+        while (p < end && *p != '\n') ++p;
+        e = p;
+        if (p < end) ++p;
+        return true;
     }
-    return !line.empty();
-}
+};
 
 // six numbers from one line, as the converter's readLine (stringstream >> double)
-static bool six(const std::string& line, double f[6]) {
-    const char* p = line.c_str();
+static bool six(const char* b, const char* e, double f[6]) {
+    char buf[512];
+    const size_t n = std::min((size_t)(e - b), sizeof buf - 1);
+    std::memcpy(buf, b, n);
+    buf[n] = 0;
+    const char* p = buf;
     for (int i = 0; i < 6; i++) {
-        char* e = nullptr;
-        f[i] = std::strtod(p, &e);
-        if (e == p) return false;
-        p = e;
+        char* q = nullptr;
+        f[i] = std::strtod(p, &q);
+        if (q == p) return false;
+        p = q;
     }
     return true;
 }
@@ -80,24 +88,26 @@ static bool six(const std::string& line, double f[6]) {
 static int parse_fin(const char* path, std::vector<FinTri>& out) {
     FILE* f = std::fopen(path, "rb");
     if (!f) return fail(RAD_ERR_IO, std::string("cannot open ") + path);
-    std::string line;
-    int rc = RAD_OK;
-    while (read_line(f, line)) {
-        if (line != "Triangle ") { rc = fail(RAD_ERR_PARSE, "a .fin record must start with \"Triangle \""); break; }
+    std::string text;
+    char chunk[1 << 16];
+    size_t got;
+    while ((got = std::fread(chunk, 1, sizeof chunk, f)) > 0) text.append(chunk, got);
+    std::fclose(f);
+    Lines L{text.data(), text.data() + text.size()};
+    const char *b, *e;
+    while (L.next(b, e)) {
+        if (std::string(b, e) != "Triangle ") return fail(RAD_ERR_PARSE, "a .fin record must start with \"Triangle \"");
         FinTri t;
         double v[6];
-        if (!read_line(f, line) || !six(line, v)) { rc = fail(RAD_ERR_PARSE, "bad colour line in .fin"); break; }
+        if (!L.next(b, e) || !six(b, e, v)) return fail(RAD_ERR_PARSE, "bad colour line in .fin");
         for (int i = 0; i < 3; i++) t.fc[i] = v[i];
-        bool ok = true;
-        for (int k = 0; k < 3 && ok; k++) {
-            ok = read_line(f, line) && six(line, v);
+        for (int k = 0; k < 3; k++) {
+            if (!L.next(b, e) || !six(b, e, v)) return fail(RAD_ERR_PARSE, "bad vertex line in .fin");
             for (int i = 0; i < 3; i++) { t.v[k][i] = v[i]; t.n[k][i] = v[i + 3]; }
         }
-        if (!ok) { rc = fail(RAD_ERR_PARSE, "bad vertex line in .fin"); break; }
         out.push_back(t);
     }
-    std::fclose(f);
-    return rc;
+    return RAD_OK;
 }
 
 // the same triangles from a scene in memory: what write_fin prints, read back
