@@ -132,7 +132,7 @@ def _scene_file(tmp):
     return sc, sc.write(os.path.join(tmp, "config2.tri"))
 
 
-def cpu_reference(tri, argv, warmup, steps, prefer_ref=True):
+def cpu_reference(tri, argv, warmup, steps, prefer_ref=True, jobs=None):
     """Time the reference's CPU solver (or the C restatement) over steps
     [warmup, warmup+steps) from its per-step timestamps."""
     sys.path.insert(0, os.path.join(REPO, "oracle"))
@@ -144,7 +144,7 @@ def cpu_reference(tri, argv, warmup, steps, prefer_ref=True):
         except Exception:
             pass
     if prefer_ref and os.path.exists(runner.REF32):
-        binary, kind, jobs = runner.REF32, "reference", cores
+        binary, kind, jobs = runner.REF32, "reference", (jobs or cores)
     else:
         runner.build_oracle()
         binary, kind, jobs = runner.ORACLE32, "port", 1
@@ -408,6 +408,7 @@ def main():
     # ---- timed region: W warm-up steps, K timed steps, L2 flushed before each
     dev = capi.Device(scene, tree, opts, local)
     dev.run(args.warmup)
+    unshot_start = dev.stats()["unshot_power"]
     barrier()
     total_ms = 0.0
     done = 0
@@ -421,6 +422,7 @@ def main():
     barrier()
     worst_ms = max_over_ranks(total_ms)
     # steady state without the flush (graph chunks of 32 steps)
+    unshot_end = dev.stats()["unshot_power"]
     n_ss, _, ms_ss = dev.run_timed(args.steps)
     st_main = dev.stats()
     dev.close()
@@ -505,6 +507,12 @@ def main():
             cpu = {"value": None, "unit": "shots/s", "cores": _nproc(), "kind": "reference",
                    "sample": f"failed: {exc}"}
         cpu = {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")}
+        if cpu["kind"] == "reference" and cpu["cores"] > 1:
+            try:
+                one = cpu_reference(tri, argv, 2, 12, jobs=1)
+                cpu["one_thread"] = {k: one[k] for k in ("value", "cores", "sample")}
+            except Exception as exc:
+                cpu["one_thread"] = {"value": None, "sample": f"failed: {exc}"}
 
     line = {
         "metric": "shots/s", "value": value, "unit": "shots/s", "n_gpus": world, "steps": done,
@@ -515,6 +523,8 @@ def main():
                    "parallelism": f"replicas x{world}", "host_prep_s": round(host_prep_s, 3)},
         "rays_per_s": d["rays"] / (worst_ms / 1000.0) if worst_ms > 0 else None,
         "rays_per_step": d["rays"] / max(done, 1),
+        "unshot_power": {"after_warmup": unshot_start, "after_timed_steps": unshot_end,
+                         "note": "FP64 total of (dB_r+dB_g+dB_b)*area over live slots (convergence monitor)"},
         "steady_state": {"value": n_ss / (ms_ss / 1000.0) if ms_ss > 0 else None, "unit": "shots/s",
                          "note": "graph chunks of 32 steps, no L2 flush", "steps": n_ss},
         "kernels_ms_per_step": {"k_setup": setup_ms / max(done, 1), "k_shoot": shoot_ms / max(done, 1)},

@@ -33,6 +33,7 @@
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "capi_internal.h"
@@ -273,6 +274,41 @@ k_setup(Slots<T> S, Shooter<T>* shooters, State* st, const Partial* __restrict__
     }
 }
 
+// ------------------------------------------------------------------ unshot power
+// The total unshot power, sum over live slots of (dB_r + dB_g + dB_b) * area,
+// in FP64: each thread sums its slots in index order, each CTA reduces in a
+// fixed tree, one CTA adds the CTA partials in order -- the same value on
+// every call for the same state.  A monitor only: selection keeps the
+// reference's FP32 key.
+constexpr int kUnshotCtas = 304, kUnshotThreads = 256;
+
+template <typename T>
+__global__ void __launch_bounds__(kUnshotThreads) k_unshot(Slots<T> S, double* part) {
+    __shared__ double red[kUnshotThreads];
+    double acc = 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < S.n; i += gridDim.x * blockDim.x) {
+        const Q4<T> fr = S.frgb[i];
+        if ((int)fr.w < 0) continue;
+        const Q4<T> db = S.deltaB[i];
+        acc += ((double)db.x + (double)db.y + (double)db.z) * (double)S.ctr[i].w;
+    }
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    for (int w = kUnshotThreads / 2; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) part[blockIdx.x] = red[0];
+}
+
+__global__ void k_unshot_total(const double* part, int n, double* out) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        double t = 0;
+        for (int i = 0; i < n; i++) t += part[i];
+        *out = t;
+    }
+}
+
 // ------------------------------------------------------------------ queries
 template <typename T>
 __global__ void k_ray_hit(Grid<T> G, const T* __restrict__ p, const T* __restrict__ v, const int* __restrict__ ban,
@@ -369,6 +405,7 @@ struct DevBase {
 
 template <typename T>
 struct DevImpl : DevBase {
+    using Real = T;
     int device = 0;
     cudaStream_t stream = nullptr;
     Slots<T> S{};
@@ -376,6 +413,7 @@ struct DevImpl : DevBase {
     Shooter<T>* d_shooters = nullptr;
     State* d_state = nullptr;
     Partial* d_part = nullptr;
+    double* d_unshot = nullptr;   // kUnshotCtas partials, then the total
     int* d_trace = nullptr;
     long long trace_cap = 0;
     int n_cta = 0;
@@ -468,7 +506,7 @@ int upload(const Scene<T>& s, const Octree<T>& o, const rad_options& opt, int de
     int *d_heavy, *d_stamp;
     if ((rc = d.alloc(&d.d_shooters, (size_t)d.P)) || (rc = d.alloc(&d.d_state, 1)) ||
         (rc = d.alloc(&d.d_part, (size_t)d.n_cta)) || (rc = d.alloc(&d_heavy, 2 * (size_t)n_groups)) ||
-        (rc = d.alloc(&d_stamp, (size_t)n_groups)))
+        (rc = d.alloc(&d_stamp, (size_t)n_groups)) || (rc = d.alloc(&d.d_unshot, (size_t)kUnshotCtas + 1)))
         return rc;
     CU(cudaMemsetAsync(d_stamp, 0xff, (size_t)n_groups * sizeof(int), d.stream));
     d.trace_cap = 1 << 16;
@@ -843,6 +881,13 @@ int rad_dev_stats(const rad_dev* h, rad_stats* st) {
         st->converged = d.host.done;
         st->n_slots = d.S.n;
         st->device_bytes = (int64_t)(d.bytes + d.trace_cap * 4);
+        using TT = typename std::remove_reference<decltype(d)>::type::Real;
+        k_unshot<TT><<<kUnshotCtas, kUnshotThreads, 0, d.stream>>>(d.S, d.d_unshot);
+        k_unshot_total<<<1, 32, 0, d.stream>>>(d.d_unshot, kUnshotCtas, d.d_unshot + kUnshotCtas);
+        CU(cudaGetLastError());
+        CU(cudaMemcpyAsync(&st->unshot_power, d.d_unshot + kUnshotCtas, sizeof(double), cudaMemcpyDeviceToHost,
+                           d.stream));
+        CU(cudaStreamSynchronize(d.stream));
         return RAD_OK;
     };
     int rc = h->d32 ? go(*h->d32) : go(*h->d64);

@@ -357,10 +357,10 @@ int main(int argc, char* argv[]) {
         double dt = ts1 - ts0;
         fprintf(stderr,
                 "[" KGRN "GPU" KWHT "] steps %lld shots %lld rays %lld in %f s: %.1f shots/s, %.3e rays/s, "
-                "precision re-steps %lld, walk-cap hits %lld, device memory %.1f MB\n",
+                "precision re-steps %lld, walk-cap hits %lld, device memory %.1f MB, unshot power %.6e\n",
                 (long long)st.steps, (long long)st.shots, (long long)st.rays, dt, dt > 0 ? st.shots / dt : 0.0,
                 dt > 0 ? st.rays / dt : 0.0, (long long)st.prec_steps, (long long)st.walk_cap_hits,
-                st.device_bytes / 1e6);
+                st.device_bytes / 1e6, st.unshot_power);
     }
     rad_dev_destroy(dev);
     rad_octree_free(tree);

@@ -54,7 +54,8 @@ class Stats(C.Structure):
     _fields_ = [("steps", C.c_int64), ("shots", C.c_int64), ("rays", C.c_int64), ("rays_ref", C.c_int64),
                 ("cells", C.c_int64), ("tri_tests", C.c_int64), ("se_tests", C.c_int64),
                 ("prec_steps", C.c_int64), ("walk_cap_hits", C.c_int64), ("converged", C.c_int32),
-                ("n_slots", C.c_int32), ("device_bytes", C.c_int64), ("walk_loops", C.c_int64)]
+                ("n_slots", C.c_int32), ("device_bytes", C.c_int64), ("walk_loops", C.c_int64),
+                ("unshot_power", C.c_double)]
 
 
 class RadError(RuntimeError):

@@ -99,6 +99,9 @@ typedef struct rad_stats {
     int64_t device_bytes;   /* device memory held by the handle */
     int64_t walk_loops;     /* walks stopped because their state repeated: the reference's
                                RayHitted never returns on these (ray treated as blocked) */
+    double unshot_power;    /* sum over live slots of (dB_r + dB_g + dB_b) * area, reduced in
+                               FP64 in a fixed order: the convergence monitor (rad_dev_stats
+                               only; selection keeps the reference's FP32 key, rad.cpp:394) */
 } rad_stats;
 
 void rad_options_default(rad_options* o);

@@ -256,3 +256,35 @@ def test_hall_bounded_steps_equal_oracle(built, workdir):
     assert v["n"] == ref["dump"]["n"] == 422429
     for k in ("accB", "deltaB"):
         assert same_bits(v[k], ref["dump"][k]), k
+
+
+@pytest.mark.parametrize("fp64", [False, True])
+def test_unshot_power_monitor(built, workdir, fp64):
+    """rad_stats.unshot_power: the FP64 total of (dB_r + dB_g + dB_b) * area over
+    live slots, reduced on the device in a fixed order.  Equal to the same sum
+    over the downloaded slots (to summation-order rounding), the same on
+    repeated calls, and non-increasing from step to step (each step zeroes the
+    shooter's unshot energy and passes on at most a reflectance < 1 of it)."""
+    sc = scenes.room_with_boxes(12, 6, 2, seed=7, size=30.0)
+    tri = sc.write(os.path.join(workdir, f"unshot{int(fp64)}.tri"))
+    o = capi.options_from_argv(sc.argv({"-triangle": "4000"}), precision=64 if fp64 else 32)
+    scene = capi.Scene.load(tri, o)
+    tree = capi.Octree(scene, 2)
+    scene.init()
+    scene.prepartition()
+    dv = capi.Device(scene, tree, o)
+    prev = None
+    for _ in range(6):
+        dv.run(7)
+        a = dv.stats()["unshot_power"]
+        assert dv.stats()["unshot_power"] == a
+        dv.download(scene)
+        v = scene.view()
+        live = v["parent"] >= 0
+        db = v["deltaB"].astype(np.float64)
+        want = float(np.sum((db[:, 0] + db[:, 1] + db[:, 2])[live] * v["area"].astype(np.float64)[live]))
+        assert abs(a - want) <= 1e-12 * abs(want)
+        if prev is not None:
+            assert a <= prev
+        prev = a
+    dv.close()
