@@ -55,12 +55,16 @@ namespace dev {
 #define RAD_SHOOT_MIN_BLOCKS 3
 #endif
 // a group is split in the next step when its item took longer than this
-// many SM cycles (a split item: the second figure)
-#ifndef RAD_HEAVY_CYCLES
-#define RAD_HEAVY_CYCLES 110000
+// fraction of the step (an item that was already split: the second figure)
+#ifndef RAD_HEAVY_FRAC
+#define RAD_HEAVY_FRAC 0.55
 #endif
-#ifndef RAD_HEAVY_CYCLES_SPLIT
-#define RAD_HEAVY_CYCLES_SPLIT 55000
+#ifndef RAD_HEAVY_FRAC_SPLIT
+#define RAD_HEAVY_FRAC_SPLIT 0.27
+#endif
+// ... and longer than this multiple of the step's mean group time
+#ifndef RAD_HEAVY_MEAN_MULT
+#define RAD_HEAVY_MEAN_MULT 2.5
 #endif
 // lanes per corner in a heavy group's items, and slots per item
 #ifndef RAD_HEAVY_LANES
@@ -77,6 +81,7 @@ k_shoot(Slots<T> S, Grid<T> G, Shooter<T>* shooters, State* st, Partial* __restr
     __shared__ int wslot[kShootThreads / 32];
     __shared__ int ndone;
     if (st->done || st->paused) return;
+    if (FUSED && threadIdx.x == 0) atomicMin(&st->t_start, global_ns());
     const int nsh = st->nsh;
     Shooter<T>* sh = reinterpret_cast<Shooter<T>*>(smem);
     T* thr = reinterpret_cast<T*>(smem + kMaxShooterBytes<T>(nsh));
@@ -105,7 +110,7 @@ k_shoot(Slots<T> S, Grid<T> G, Shooter<T>* shooters, State* st, Partial* __restr
         if (lane == 0) g = atomicAdd(&st->work, 1);
         g = __shfl_sync(kFull, g, 0);
         int grp;
-        const long long t_item = clock64();
+        const unsigned long long t_item = global_ns();
         if constexpr (!COUNT) {
             if (g < n_heavy_items) {
                 grp = st->heavy[(s & 1) * n_groups + g / kHeavyItems];
@@ -121,8 +126,12 @@ k_shoot(Slots<T> S, Grid<T> G, Shooter<T>* shooters, State* st, Partial* __restr
             shoot_group<T, COUNT>(S, Gs, sh, nsh, grp, lane, conv, kk, ks, c);
         }
         if (split && lane == 0) {
-            const long long dt = clock64() - t_item;
-            if (dt > (g < n_heavy_items ? st->heavy_cycles_split : st->heavy_cycles) &&
+            const long long dt = (long long)(global_ns() - t_item);
+            if (g >= n_heavy_items) {
+                atomicAdd(&st->item_ns, (unsigned long long)dt);
+                atomicAdd(&st->items, 1u);
+            }
+            if (dt > (g < n_heavy_items ? st->heavy_ns_split : st->heavy_ns) &&
                 atomicMax(&st->stamp[grp], s + 1) < s + 1) {
                 const int q = atomicAdd(&st->heavy_n[(s + 1) & 1], 1);
                 st->heavy[((s + 1) & 1) * n_groups + q] = grp;
@@ -180,6 +189,16 @@ k_shoot(Slots<T> S, Grid<T> G, Shooter<T>* shooters, State* st, Partial* __restr
         st->work = 0;
         st->ctas_done = 0;
         st->heavy_n[(steps + 1) & 1] = 0;   // consumed by this step, refilled by the next
+        // the next step's split limits, from this step's duration
+        const long long took = (long long)(global_ns() - st->t_start);
+        if (nsh > 0 && !COUNT && st->items > 0) {
+            const double mean = (double)st->item_ns / (double)st->items;
+            st->heavy_ns = (long long)fmax(RAD_HEAVY_FRAC * (double)took, RAD_HEAVY_MEAN_MULT * mean);
+            st->heavy_ns_split = (long long)(RAD_HEAVY_FRAC_SPLIT * (double)took);
+        }
+        st->t_start = ~0ull;
+        st->item_ns = 0;
+        st->items = 0;
     }
 }
 
@@ -518,8 +537,9 @@ int upload(const Scene<T>& s, const Octree<T>& o, const rad_options& opt, int de
     st.heavy = d_heavy;
     st.stamp = d_stamp;
     st.heavy_on = d.P == 1;
-    st.heavy_cycles = RAD_HEAVY_CYCLES;
-    st.heavy_cycles_split = RAD_HEAVY_CYCLES_SPLIT;
+    st.heavy_ns = 0x7fffffffffffffffLL;   // no split before a step has been timed
+    st.heavy_ns_split = 0x7fffffffffffffffLL;
+    st.t_start = ~0ull;
     CU(cudaMemcpyAsync(d.d_state, &st, sizeof st, cudaMemcpyHostToDevice, d.stream));
     CU(cudaMemsetAsync(d.d_shooters, 0, sizeof(Shooter<T>) * d.P, d.stream));
     CU(cudaMemsetAsync(d.d_part, 0, sizeof(Partial) * d.n_cta, d.stream));

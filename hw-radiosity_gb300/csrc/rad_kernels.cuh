@@ -234,17 +234,29 @@ struct State {
     long long trace_cap;
     int* trace;
     unsigned long long rays, rays_ref, cells, tris, se, prec, capped, loops;
-    // Groups whose item took longer than heavy_cycles (split items:
-    // heavy_cycles_split) in step s are listed in heavy[(s+1)&1] and stamped
+    // Groups whose item took longer than heavy_ns (split items:
+    // heavy_ns_split) in step s are listed in heavy[(s+1)&1] and stamped
     // s+1; step s+1 hands each out first, as items of a few slots whose
-    // corners are cast by several lanes each.  Only the schedule depends on
-    // it, not the results.
+    // corners are cast by several lanes each.  A group is split when it is
+    // long against both the whole step and the typical group: the limit is
+    // the larger of a fraction of the previous step's duration (t_start: its
+    // first CTA, by %globaltimer) and a multiple of its mean group time
+    // (item_ns / items over the groups shot whole).  Only the schedule
+    // depends on it, not the results.
     int* heavy;             // 2 x n_groups
     int* stamp;             // per group: the last step it was split in (-1: never)
     int heavy_n[2];
     int heavy_on;           // one shooter per step (the fused kernel)
-    long long heavy_cycles, heavy_cycles_split;
+    long long heavy_ns, heavy_ns_split;
+    unsigned long long t_start, item_ns;
+    unsigned items;
 };
+
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
 
 struct Cnt { unsigned rays, rays_ref, cells, tris, se, prec, capped, loops; };
 
