@@ -440,6 +440,12 @@ __device__ __forceinline__ int walk_lanes(const Grid<T>& G, const T p[3], const 
             continue;
         }
         const int b = cr.b, e = cr.e;
+        if (b == e) {                // empty list: no hit, every lane knows
+            prev = leaf;
+            t = next_t(G, p, v, cr.lo, cr.hi);
+            q0 = p[0] + t * v[0]; q1 = p[1] + t * v[1]; q2 = p[2] + t * v[2];
+            continue;
+        }
         T tmin = (T)1000000.0;
         int bk = -1;
         bool nan = false;
