@@ -66,6 +66,11 @@ namespace dev {
 #ifndef RAD_HEAVY_MEAN_MULT
 #define RAD_HEAVY_MEAN_MULT 2.5
 #endif
+// a group shot whole that took longer than this multiple of the step's mean
+// group time starts early in the next step
+#ifndef RAD_EARLY_MEAN_MULT
+#define RAD_EARLY_MEAN_MULT 1.5
+#endif
 // lanes per corner in a heavy group's items, and slots per item
 #ifndef RAD_HEAVY_LANES
 #define RAD_HEAVY_LANES 4
@@ -105,6 +110,7 @@ k_shoot(Slots<T> S, Grid<T> G, Shooter<T>* shooters, State* st, Partial* __restr
     const bool split = !COUNT && FUSED && st->heavy_on;
     const int s = (int)st->steps;
     const int n_heavy_items = split ? st->heavy_n[s & 1] * kHeavyItems : 0;
+    const int n_early = split ? st->early_n[s & 1] : 0;
     for (;;) {
         int g = 0;
         if (lane == 0) g = atomicAdd(&st->work, 1);
@@ -120,8 +126,14 @@ k_shoot(Slots<T> S, Grid<T> G, Shooter<T>* shooters, State* st, Partial* __restr
             }
         }
         if (g >= n_heavy_items) {
-            grp = g - n_heavy_items;
-            if (grp >= n_groups) break;
+            const int j = g - n_heavy_items;
+            if (j < n_early) {
+                grp = st->early[(s & 1) * n_groups + j];
+            } else {
+                grp = j - n_early;
+                if (grp >= n_groups) break;
+                if (split && __ldcg(&st->estamp[grp]) >= s) continue;   // it was in the early part
+            }
             if (split && __ldcg(&st->stamp[grp]) >= s) continue;   // its items are in the heavy part
             shoot_group<T, COUNT>(S, Gs, sh, nsh, grp, lane, conv, kk, ks, c);
         }
@@ -131,10 +143,15 @@ k_shoot(Slots<T> S, Grid<T> G, Shooter<T>* shooters, State* st, Partial* __restr
                 atomicAdd(&st->item_ns, (unsigned long long)dt);
                 atomicAdd(&st->items, 1u);
             }
-            if (dt > (g < n_heavy_items ? st->heavy_ns_split : st->heavy_ns) &&
-                atomicMax(&st->stamp[grp], s + 1) < s + 1) {
-                const int q = atomicAdd(&st->heavy_n[(s + 1) & 1], 1);
-                st->heavy[((s + 1) & 1) * n_groups + q] = grp;
+            if (dt > (g < n_heavy_items ? st->heavy_ns_split : st->heavy_ns)) {
+                if (atomicMax(&st->stamp[grp], s + 1) < s + 1) {
+                    const int q = atomicAdd(&st->heavy_n[(s + 1) & 1], 1);
+                    st->heavy[((s + 1) & 1) * n_groups + q] = grp;
+                }
+            } else if (g >= n_heavy_items && dt > st->early_ns) {
+                st->estamp[grp] = s + 1;
+                const int q = atomicAdd(&st->early_n[(s + 1) & 1], 1);
+                st->early[((s + 1) & 1) * n_groups + q] = grp;
             }
         }
     }
@@ -189,12 +206,14 @@ k_shoot(Slots<T> S, Grid<T> G, Shooter<T>* shooters, State* st, Partial* __restr
         st->work = 0;
         st->ctas_done = 0;
         st->heavy_n[(steps + 1) & 1] = 0;   // consumed by this step, refilled by the next
+        st->early_n[(steps + 1) & 1] = 0;
         // the next step's split limits, from this step's duration
         const long long took = (long long)(global_ns() - st->t_start);
         if (nsh > 0 && !COUNT && st->items > 0) {
             const double mean = (double)st->item_ns / (double)st->items;
             st->heavy_ns = (long long)fmax(RAD_HEAVY_FRAC * (double)took, RAD_HEAVY_MEAN_MULT * mean);
             st->heavy_ns_split = (long long)(RAD_HEAVY_FRAC_SPLIT * (double)took);
+            st->early_ns = (long long)(RAD_EARLY_MEAN_MULT * mean);
         }
         st->t_start = ~0ull;
         st->item_ns = 0;
@@ -522,12 +541,14 @@ int upload(const Scene<T>& s, const Octree<T>& o, const rad_options& opt, int de
         d.n_cta = std::max(1, std::min(want, std::max(1, sms * per_sm)));
     }
     const int n_groups = (n + kSlotsPerWarp - 1) / kSlotsPerWarp;
-    int *d_heavy, *d_stamp;
+    int *d_heavy, *d_stamp, *d_early, *d_estamp;
     if ((rc = d.alloc(&d.d_shooters, (size_t)d.P)) || (rc = d.alloc(&d.d_state, 1)) ||
         (rc = d.alloc(&d.d_part, (size_t)d.n_cta)) || (rc = d.alloc(&d_heavy, 2 * (size_t)n_groups)) ||
-        (rc = d.alloc(&d_stamp, (size_t)n_groups)) || (rc = d.alloc(&d.d_unshot, (size_t)kUnshotCtas + 1)))
+        (rc = d.alloc(&d_stamp, (size_t)n_groups)) || (rc = d.alloc(&d.d_unshot, (size_t)kUnshotCtas + 1)) ||
+        (rc = d.alloc(&d_early, 2 * (size_t)n_groups)) || (rc = d.alloc(&d_estamp, (size_t)n_groups)))
         return rc;
     CU(cudaMemsetAsync(d_stamp, 0xff, (size_t)n_groups * sizeof(int), d.stream));
+    CU(cudaMemsetAsync(d_estamp, 0xff, (size_t)n_groups * sizeof(int), d.stream));
     d.trace_cap = 1 << 16;
     CU(cudaMalloc(&d.d_trace, (size_t)d.trace_cap * 4));
     State st{};
@@ -539,6 +560,9 @@ int upload(const Scene<T>& s, const Octree<T>& o, const rad_options& opt, int de
     st.heavy_on = d.P == 1;
     st.heavy_ns = 0x7fffffffffffffffLL;   // no split before a step has been timed
     st.heavy_ns_split = 0x7fffffffffffffffLL;
+    st.early = d_early;
+    st.estamp = d_estamp;
+    st.early_ns = 0x7fffffffffffffffLL;
     st.t_start = ~0ull;
     CU(cudaMemcpyAsync(d.d_state, &st, sizeof st, cudaMemcpyHostToDevice, d.stream));
     CU(cudaMemsetAsync(d.d_shooters, 0, sizeof(Shooter<T>) * d.P, d.stream));

@@ -250,6 +250,13 @@ struct State {
     long long heavy_ns, heavy_ns_split;
     unsigned long long t_start, item_ns;
     unsigned items;
+    // Groups that took longer than early_ns without being split are stamped
+    // (estamp) and listed in early[(s+1)&1]; step s+1 hands them out right
+    // after the split items, the rest follow in slot order.
+    int* early;             // 2 x n_groups
+    int* estamp;            // per group: the last step it was listed early in (-1: never)
+    int early_n[2];
+    long long early_ns;
 };
 
 __device__ __forceinline__ unsigned long long global_ns() {
