@@ -211,9 +211,9 @@ k_shoot(Slots<T> S, Grid<T> G, Shooter<T>* shooters, State* st, Partial* __restr
         const long long took = (long long)(global_ns() - st->t_start);
         if (nsh > 0 && !COUNT && st->items > 0) {
             const double mean = (double)st->item_ns / (double)st->items;
-            st->heavy_ns = (long long)fmax(RAD_HEAVY_FRAC * (double)took, RAD_HEAVY_MEAN_MULT * mean);
-            st->heavy_ns_split = (long long)(RAD_HEAVY_FRAC_SPLIT * (double)took);
-            st->early_ns = (long long)(RAD_EARLY_MEAN_MULT * mean);
+            st->heavy_ns = (long long)fmax(st->frac * (double)took, st->mean_mult * mean);
+            st->heavy_ns_split = (long long)(st->frac_split * (double)took);
+            st->early_ns = (long long)(st->early_mult * mean);
         }
         st->t_start = ~0ull;
         st->item_ns = 0;
@@ -563,6 +563,10 @@ int upload(const Scene<T>& s, const Octree<T>& o, const rad_options& opt, int de
     st.early = d_early;
     st.estamp = d_estamp;
     st.early_ns = 0x7fffffffffffffffLL;
+    st.frac = RAD_HEAVY_FRAC;
+    st.frac_split = RAD_HEAVY_FRAC_SPLIT;
+    st.mean_mult = RAD_HEAVY_MEAN_MULT;
+    st.early_mult = RAD_EARLY_MEAN_MULT;
     st.t_start = ~0ull;
     CU(cudaMemcpyAsync(d.d_state, &st, sizeof st, cudaMemcpyHostToDevice, d.stream));
     CU(cudaMemsetAsync(d.d_shooters, 0, sizeof(Shooter<T>) * d.P, d.stream));
@@ -948,6 +952,21 @@ int rad_dev_stats(const rad_dev* h, rad_stats* st) {
         for (int64_t k = 0; k < n; k++) st->shots += tr[k] >= 0;
     }
     return RAD_OK;
+}
+
+int rad_dev_set_schedule(rad_dev* h, double split_frac, double split_frac_split, double split_mean_mult,
+                         double early_mean_mult) {
+    if (!h) return fail(RAD_ERR_ARG, "rad_dev_set_schedule: null handle");
+    if (!(split_frac >= 0) || !(split_frac_split >= 0) || !(split_mean_mult >= 0) || !(early_mean_mult >= 0))
+        return fail(RAD_ERR_ARG, "rad_dev_set_schedule: limits must be >= 0");
+    auto go = [&](auto& d) -> int {
+        CU(cudaSetDevice(d.device));
+        const double v[4] = {split_frac, split_frac_split, split_mean_mult, early_mean_mult};
+        CU(cudaMemcpyAsync(&d.d_state->frac, v, sizeof v, cudaMemcpyHostToDevice, d.stream));
+        CU(cudaStreamSynchronize(d.stream));
+        return RAD_OK;
+    };
+    return h->d32 ? go(*h->d32) : go(*h->d64);
 }
 
 int rad_dev_set_counting(rad_dev* h, int32_t on) {

@@ -257,6 +257,10 @@ struct State {
     int* estamp;            // per group: the last step it was listed early in (-1: never)
     int early_n[2];
     long long early_ns;
+    // the schedule's limits (rad_dev_set_schedule): split above
+    // max(frac * step, mean_mult * mean), keep split above frac_split * step,
+    // start early above early_mult * mean
+    double frac, frac_split, mean_mult, early_mult;
 };
 
 __device__ __forceinline__ unsigned long long global_ns() {

@@ -25,7 +25,7 @@ EXPORTS = [
     "rad_scene_view_get", "rad_scene_write_fin", "rad_scene_log", "rad_scene_free",
     "rad_octree_build", "rad_octree_info", "rad_octree_cell_coords", "rad_octree_free",
     "rad_dev_create", "rad_dev_run", "rad_dev_run_timed", "rad_dev_run_profiled", "rad_dev_download", "rad_dev_trace", "rad_dev_stats",
-    "rad_dev_set_counting", "rad_dev_ray_hit", "rad_dev_form_factors", "rad_dev_form_factors_noalloc",
+    "rad_dev_set_counting", "rad_dev_set_schedule", "rad_dev_ray_hit", "rad_dev_form_factors", "rad_dev_form_factors_noalloc",
     "rad_dev_destroy",
     "rad_batch_create", "rad_batch_run", "rad_batch_run_timed", "rad_batch_scene_stats", "rad_batch_download",
     "rad_batch_trace", "rad_batch_stats", "rad_batch_set_counting", "rad_batch_destroy",
@@ -109,6 +109,7 @@ def load(path: Optional[str] = None) -> C.CDLL:
         "rad_dev_ray_hit": (C.c_int, [vp, vp, vp, vp, i32, vp]),
         "rad_dev_form_factors": (C.c_int, [vp, i32, vp, i32, vp]),
         "rad_dev_form_factors_noalloc": (C.c_int, [vp, vp, i32, vp, i32, vp, vp]),
+        "rad_dev_set_schedule": (C.c_int, [vp, C.c_double, C.c_double, C.c_double, C.c_double]),
         "rad_dev_destroy": (None, [vp]),
         "rad_batch_create": (C.c_int, [vp, vp, vp, i32, i32, i32, P(vp)]),
         "rad_batch_run": (C.c_int, [vp, i64, P(i64), P(i32)]),
@@ -320,6 +321,11 @@ class Device:
 
     def set_counting(self, on: bool):
         _check(load().rad_dev_set_counting(self.h, 1 if on else 0))
+
+    def set_schedule(self, split_frac=0.55, split_frac_split=0.27, split_mean_mult=2.5, early_mean_mult=1.5):
+        """Limits of the single-shooter schedule (rad_dev_set_schedule); all 0
+        splits every group after the first step."""
+        _check(load().rad_dev_set_schedule(self.h, split_frac, split_frac_split, split_mean_mult, early_mean_mult))
 
     def ray_hit(self, p: np.ndarray, v: np.ndarray, ban: np.ndarray, dtype=np.float32) -> np.ndarray:
         p = np.ascontiguousarray(p, dtype).reshape(-1, 3)

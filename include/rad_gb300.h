@@ -173,6 +173,17 @@ int rad_dev_download(rad_dev* d, rad_scene* s);
 int rad_dev_trace(const rad_dev* d, int32_t* out, int64_t cap, int64_t* n);
 int rad_dev_stats(const rad_dev* d, rad_stats* st);
 /* Count cells / triangle tests / edge tests during later steps (slower). */
+/* The single-shooter schedule (no reference counterpart; results do not
+ * depend on it).  A 10-slot group whose work item took longer than
+ * max(split_frac * step time, split_mean_mult * mean group time) in one step
+ * is shot in the next as 2-slot items with 4 lanes per corner; an item that
+ * was already split stays split above split_frac_split * step time; a group
+ * over early_mean_mult * mean group time is handed out first.  Defaults
+ * 0.55, 0.27, 2.5, 1.5.  All zero splits every group after the first step
+ * (tests use this to run the 4-lane walk everywhere); large values turn it
+ * off. */
+int rad_dev_set_schedule(rad_dev* d, double split_frac, double split_frac_split, double split_mean_mult,
+                         double early_mean_mult);
 int rad_dev_set_counting(rad_dev* d, int32_t on);
 /* Batched RayHitted (src/raycast.cpp:335-360): for each i, the triangle the
  * walk from p[i] along v[i] (not normalised) stops at, skipping ban[i]; -1 if

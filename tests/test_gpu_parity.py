@@ -21,13 +21,15 @@ pytestmark = pytest.mark.gpu
 CASES = sorted(k for k, v in golden_index().items() if not v.get("adaptive"))
 
 
-def _solve(tri, argv, fp64=False, chunks=None, **kw):
+def _solve(tri, argv, fp64=False, chunks=None, schedule=None, **kw):
     o = capi.options_from_argv(argv, precision=64 if fp64 else 32, **kw)
     sc = capi.Scene.load(tri, o)
     tree = capi.Octree(sc, 4)
     sc.init()
     sc.prepartition()
     dv = capi.Device(sc, tree, o)
+    if schedule is not None:
+        dv.set_schedule(*schedule)
     if chunks:
         total = 0
         for c in chunks:
@@ -288,3 +290,51 @@ def test_unshot_power_monitor(built, workdir, fp64):
             assert a <= prev
         prev = a
     dv.close()
+
+
+
+SPLIT_ALWAYS = (0.0, 0.0, 0.0, 0.0)   # every group shot as 2-slot items, 4 lanes per corner, from step 2 on
+SPLIT_NEVER = (1e9, 1e9, 1e9, 1e9)
+
+
+@pytest.mark.parametrize("name", [c for c in CASES if not golden_index()[c].get("P", 1) > 1])
+@pytest.mark.parametrize("schedule", [SPLIT_ALWAYS, SPLIT_NEVER], ids=["split_always", "split_never"])
+def test_schedule_does_not_change_results(built, workdir, name, schedule):
+    """The schedule (which groups are split into 4-lane items, which start
+    early) changes only timing: with every group split from the second step
+    on (the 4-lane walk and its NaN fallback everywhere, FP32 and FP64) and
+    with nothing split, the results equal the reference fixture bit for bit."""
+    tri, argv, idx = write_case(name, workdir)
+    sc, dv, steps, conv = _solve(tri, argv, fp64=idx["fp64"], schedule=schedule)
+    g = golden(name)
+    assert conv
+    assert steps == idx["steps"]
+    assert np.array_equal(dv.trace(), g["trace"])
+    v = sc.view()
+    for k in ("parent", "p", "accB", "deltaB", "nb"):
+        assert same_bits(v[k], g[k]), k
+
+
+def test_split_schedule_on_hall_steps(built, workdir):
+    """The 422k-triangle hall with every group split, 40 steps: equal to the
+    same steps with nothing split (the unsplit path is held to the oracle by
+    test_hall_bounded_steps_equal_oracle)."""
+    sc_gen = scenes.hall()
+    tri = sc_gen.write(os.path.join(workdir, "hall_split.tri"))
+    out = []
+    for sched in (SPLIT_ALWAYS, SPLIT_NEVER):
+        o = capi.options_from_argv(sc_gen.argv())
+        sc = capi.Scene.load(tri, o)
+        tree = capi.Octree(sc, 8)
+        sc.init()
+        sc.prepartition()
+        dv = capi.Device(sc, tree, o)
+        dv.set_schedule(*sched)
+        dv.run(40)
+        dv.download(sc)
+        v = sc.view()
+        out.append((dv.trace().copy(), v["accB"].copy(), v["deltaB"].copy()))
+        dv.close()
+    assert np.array_equal(out[0][0], out[1][0])
+    assert same_bits(out[0][1], out[1][1])
+    assert same_bits(out[0][2], out[1][2])
