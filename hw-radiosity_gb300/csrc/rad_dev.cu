@@ -157,41 +157,50 @@ k_shoot(Slots<T> S, Grid<T> G, Shooter<T>* shooters, State* st, Partial* __restr
     }
     warp_max(kk, ks);
     flush_counters<COUNT>(st, c, lane);
-    int last = 0;
     if (lane == 0) {
         wkey[wid] = kk;
         wslot[wid] = ks;
-        __threadfence_block();
-        last = atomicAdd(&ndone, 1) == kShootThreads / 32 - 1;
     }
-    if (!__shfl_sync(kFull, last, 0)) return;
-    // the CTA's last warp: the CTA partial
-    if (lane == 0) {
-        volatile unsigned long long* vk = wkey;
-        volatile int* vs = wslot;
+    // The queue is empty: the CTA's warps meet (the early ones have nothing
+    // left to do) and thread 0 writes the CTA partial.
+    __syncthreads();
+    if (threadIdx.x == 0) {
         unsigned long long bk = 0;
         int bs = -1;
         for (int w = 0; w < kShootThreads / 32; w++)
-            if (part_less(bk, bs, vk[w], vs[w])) { bk = vk[w]; bs = vs[w]; }
+            if (part_less(bk, bs, wkey[w], wslot[w])) { bk = wkey[w]; bs = wslot[w]; }
         part[blockIdx.x].key = bk;
         part[blockIdx.x].slot = bs;
+        if (FUSED) {
+            __threadfence();
+            ndone = atomicAdd(&st->ctas_done, 1) == (int)gridDim.x - 1;
+        }
     }
     if (!FUSED) return;
-    __threadfence();
-    last = 0;
-    if (lane == 0) last = atomicAdd(&st->ctas_done, 1) == (int)gridDim.x - 1;
-    if (!__shfl_sync(kFull, last, 0)) return;
-    // the grid's last warp: select the next step's shooter (listCanditate for one shooter)
+    __syncthreads();
+    if (!ndone) return;
+    // the grid's last CTA: select the next step's shooter (listCanditate for
+    // one shooter), every thread reading a few CTA partials
     __threadfence();
     kk = 0;
     ks = -1;
-    for (int q = lane; q < (int)gridDim.x; q += 32) {
+    for (int q = threadIdx.x; q < (int)gridDim.x; q += blockDim.x) {
         const unsigned long long qk = __ldcg(&part[q].key);
         const int qs = __ldcg(&part[q].slot);
         if (part_less(kk, ks, qk, qs)) { kk = qk; ks = qs; }
     }
     warp_max(kk, ks);
+    __syncthreads();          // wkey / wslot are reused
     if (lane == 0) {
+        wkey[wid] = kk;
+        wslot[wid] = ks;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        kk = 0;
+        ks = -1;
+        for (int w = 0; w < kShootThreads / 32; w++)
+            if (part_less(kk, ks, wkey[w], wslot[w])) { kk = wkey[w]; ks = wslot[w]; }
         long long steps = st->steps + (nsh > 0 ? 1 : 0);    // the step just shot is complete
         if (!kk) {
             st->done = 1;
