@@ -111,10 +111,16 @@ k_shoot(Slots<T> S, Grid<T> G, Shooter<T>* shooters, State* st, Partial* __restr
     const int s = (int)st->steps;
     const int n_heavy_items = split ? st->heavy_n[s & 1] * kHeavyItems : 0;
     const int n_early = split ? st->early_n[s & 1] : 0;
+    // each warp's first item is its own index; later ones come from the queue
+    const int n_warps = (int)gridDim.x * (kShootThreads / 32);
+    int first = (int)blockIdx.x * (kShootThreads / 32) + wid;
     for (;;) {
-        int g = 0;
-        if (lane == 0) g = atomicAdd(&st->work, 1);
-        g = __shfl_sync(kFull, g, 0);
+        int g = first;
+        if (first < 0) {
+            if (lane == 0) g = atomicAdd(&st->work, 1) + n_warps;
+            g = __shfl_sync(kFull, g, 0);
+        }
+        first = -1;
         int grp;
         const unsigned long long t_item = global_ns();
         if constexpr (!COUNT) {
