@@ -330,8 +330,8 @@ k_setup(Slots<T> S, Shooter<T>* shooters, State* st, const Partial* __restrict__
 // ------------------------------------------------------------------ unshot power
 // The total unshot power, sum over live slots of (dB_r + dB_g + dB_b) * area,
 // in FP64: each thread sums its slots in index order, each CTA reduces in a
-// fixed tree, one CTA adds the CTA partials in order -- the same value on
-// every call for the same state.  A monitor only: selection keeps the
+// fixed tree, one warp adds the CTA partials in a fixed order -- the same
+// value on every call for the same state.  A monitor only: selection keeps the
 // reference's FP32 key.
 constexpr int kUnshotCtas = 304, kUnshotThreads = 256;
 
@@ -354,12 +354,14 @@ __global__ void __launch_bounds__(kUnshotThreads) k_unshot(Slots<T> S, double* p
     if (threadIdx.x == 0) part[blockIdx.x] = red[0];
 }
 
+// one warp: lane l adds partials l, l+32, ... in order, then a fixed tree
 __global__ void k_unshot_total(const double* part, int n, double* out) {
-    if (threadIdx.x == 0 && blockIdx.x == 0) {
-        double t = 0;
-        for (int i = 0; i < n; i++) t += part[i];
-        *out = t;
-    }
+    const int lane = threadIdx.x & 31;
+    double t = 0;
+    for (int i = lane; i < n; i += 32) t += part[i];
+#pragma unroll
+    for (int d = 16; d; d >>= 1) t += __shfl_xor_sync(kFull, t, d);
+    if (threadIdx.x == 0) *out = t;
 }
 
 // ------------------------------------------------------------------ queries
