@@ -51,9 +51,6 @@ namespace dev {
 // also does the next step's selection -- it reduces the per-CTA partials,
 // builds the next shooter record and advances the step -- so a step is one
 // kernel.  Several shooters per step keep the separate k_setup.
-#ifndef RAD_SHOOT_MIN_BLOCKS
-#define RAD_SHOOT_MIN_BLOCKS 3
-#endif
 // a group is split in the next step when its item took longer than this
 // fraction of the step (an item that was already split: the second figure)
 #ifndef RAD_HEAVY_FRAC
@@ -71,15 +68,21 @@ namespace dev {
 #ifndef RAD_EARLY_MEAN_MULT
 #define RAD_EARLY_MEAN_MULT 1.5
 #endif
-// lanes per corner in a heavy group's items, and slots per item
-#ifndef RAD_HEAVY_LANES
-#define RAD_HEAVY_LANES 4
-#endif
-constexpr int kHeavyLanes = RAD_HEAVY_LANES;
-constexpr int kHeavySlots = 32 / (3 * kHeavyLanes);
-constexpr int kHeavyItems = (kSlotsPerWarp + kHeavySlots - 1) / kHeavySlots;   // items per heavy group
-template <typename T, bool COUNT, bool FUSED>
-__global__ void __launch_bounds__(kShootThreads, RAD_SHOOT_MIN_BLOCKS)
+// Two forms of the single-shooter kernel, picked per scene (layout):
+//   1 (tail-bound: a step is about one wave of groups) -- 3 CTAs per SM, 80
+//     registers, a split group's items cast each corner with 4 lanes that
+//     share the list scans, so a long walk ends sooner;
+//   2 (throughput-bound: many groups per warp, e.g. 400k triangles) -- 4 CTAs
+//     per SM, 64 registers, split items keep one lane per corner (3 slots
+//     per item) so the walk is inlined once and more warps hide latency.
+// Measured: the 61k-triangle room 9.7k vs 7.7k shots/s (flushed) in form 1
+// vs 2; the 422k-triangle hall 841 vs 998 shots/s.
+template <int HL>
+__host__ __device__ constexpr int heavy_slots() { return HL == 1 ? 3 : 32 / (3 * HL); }
+template <int HL>
+__host__ __device__ constexpr int heavy_items() { return (kSlotsPerWarp + heavy_slots<HL>() - 1) / heavy_slots<HL>(); }
+template <typename T, bool COUNT, bool FUSED, int MINB, int HL>
+__global__ void __launch_bounds__(kShootThreads, MINB)
 k_shoot(Slots<T> S, Grid<T> G, Shooter<T>* shooters, State* st, Partial* __restrict__ part, T conv) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ unsigned long long wkey[kShootThreads / 32];
@@ -109,6 +112,7 @@ k_shoot(Slots<T> S, Grid<T> G, Shooter<T>* shooters, State* st, Partial* __restr
     // the queue: the heavy groups' one-slot items first, then the other groups
     const bool split = !COUNT && FUSED && st->heavy_on;
     const int s = (int)st->steps;
+    constexpr int kHeavySlots = heavy_slots<HL>(), kHeavyItems = heavy_items<HL>();
     const int n_heavy_items = split ? st->heavy_n[s & 1] * kHeavyItems : 0;
     const int n_early = split ? st->early_n[s & 1] : 0;
     // each warp's first item is its own index; later ones come from the queue
@@ -121,17 +125,14 @@ k_shoot(Slots<T> S, Grid<T> G, Shooter<T>* shooters, State* st, Partial* __restr
             g = __shfl_sync(kFull, g, 0);
         }
         first = -1;
-        int grp;
+        int grp, i0, n_item;
         const unsigned long long t_item = global_ns();
-        if constexpr (!COUNT) {
-            if (g < n_heavy_items) {
-                grp = st->heavy[(s & 1) * n_groups + g / kHeavyItems];
-                const int part = (g % kHeavyItems) * kHeavySlots;
-                shoot_item<T, false, kHeavyLanes>(S, Gs, sh, nsh, grp * kSlotsPerWarp + part,
-                                                  imin(kHeavySlots, kSlotsPerWarp - part), lane, conv, kk, ks, c);
-            }
-        }
-        if (g >= n_heavy_items) {
+        if (g < n_heavy_items) {
+            grp = st->heavy[(s & 1) * n_groups + g / kHeavyItems];
+            const int part = (g % kHeavyItems) * kHeavySlots;
+            i0 = grp * kSlotsPerWarp + part;
+            n_item = imin(kHeavySlots, kSlotsPerWarp - part);
+        } else {
             const int j = g - n_heavy_items;
             if (j < n_early) {
                 grp = st->early[(s & 1) * n_groups + j];
@@ -141,7 +142,18 @@ k_shoot(Slots<T> S, Grid<T> G, Shooter<T>* shooters, State* st, Partial* __restr
                 if (split && __ldcg(&st->estamp[grp]) >= s) continue;   // it was in the early part
             }
             if (split && __ldcg(&st->stamp[grp]) >= s) continue;   // its items are in the heavy part
-            shoot_group<T, COUNT>(S, Gs, sh, nsh, grp, lane, conv, kk, ks, c);
+            i0 = grp * kSlotsPerWarp;
+            n_item = kSlotsPerWarp;
+        }
+        // one call site when every item is cast one lane per corner: the
+        // walk is inlined once, which keeps the register count down
+        if constexpr (HL == 1 || COUNT) {
+            shoot_item<T, COUNT, 1>(S, Gs, sh, nsh, i0, n_item, lane, conv, kk, ks, c);
+        } else {
+            if (g < n_heavy_items)
+                shoot_item<T, false, HL>(S, Gs, sh, nsh, i0, n_item, lane, conv, kk, ks, c);
+            else
+                shoot_item<T, COUNT, 1>(S, Gs, sh, nsh, i0, n_item, lane, conv, kk, ks, c);
         }
         if (split && lane == 0) {
             const long long dt = (long long)(global_ns() - t_item);
@@ -471,20 +483,23 @@ struct DevImpl : DevBase {
     double* d_unshot = nullptr;   // kUnshotCtas partials, then the total
     int* d_trace = nullptr;
     long long trace_cap = 0;
-    int n_cta = 0;
+    int n_cta = 0;          // CTAs of the current layout's kernel
+    int n_cta1 = 0, n_cta2 = 0;
+    int layout = 1;         // 1 tail-bound form, 2 throughput form (FP32, one shooter per step)
     int P = 1;
     T conv = 0;
     bool counting = false;
-    cudaGraphExec_t graphs[2][33] = {};   // [counting][steps per launch]
+    cudaGraphExec_t graphs[3][2][33] = {};   // [layout][counting][steps per launch]
     cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
     std::vector<void*> allocs;
     size_t bytes = 0;
     State host{};   // mirror after the last synchronisation
 
     ~DevImpl() override {
-        for (auto& row : graphs)
-            for (auto& g : row)
-                if (g) cudaGraphExecDestroy(g);
+        for (auto& plane : graphs)
+            for (auto& row : plane)
+                for (auto& g : row)
+                    if (g) cudaGraphExecDestroy(g);
         for (auto& e : ev)
             if (e) cudaEventDestroy(e);
         for (void* p : allocs) cudaFree(p);
@@ -544,23 +559,35 @@ int upload(const Scene<T>& s, const Octree<T>& o, const rad_options& opt, int de
     // per-step state; k_shoot is persistent: as many CTAs as fit at once
     d.n_thr = (int)o.thr.size();
     if (d.shoot_smem() > 48 * 1024) {
-        CU(cudaFuncSetAttribute(k_shoot<T, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)d.shoot_smem()));
-        CU(cudaFuncSetAttribute(k_shoot<T, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)d.shoot_smem()));
-        CU(cudaFuncSetAttribute(k_shoot<T, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)d.shoot_smem()));
-        CU(cudaFuncSetAttribute(k_shoot<T, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)d.shoot_smem()));
-    }
-    {
-        int sms = 0, per_sm = 0;
-        CU(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
-        CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_shoot<T, false, true>, kShootThreads, d.shoot_smem()));
-        const int n_groups = (n + kSlotsPerWarp - 1) / kSlotsPerWarp;
-        const int want = (n_groups + kShootThreads / 32 - 1) / (kShootThreads / 32);
-        d.n_cta = std::max(1, std::min(want, std::max(1, sms * per_sm)));
+        CU(cudaFuncSetAttribute(k_shoot<T, false, false, 3, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)d.shoot_smem()));
+        CU(cudaFuncSetAttribute(k_shoot<T, true, false, 3, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)d.shoot_smem()));
+        CU(cudaFuncSetAttribute(k_shoot<T, false, true, 3, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)d.shoot_smem()));
+        CU(cudaFuncSetAttribute(k_shoot<T, true, true, 3, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)d.shoot_smem()));
+        if constexpr (std::is_same<T, float>::value)
+            CU(cudaFuncSetAttribute(k_shoot<T, false, true, 4, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)d.shoot_smem()));
     }
     const int n_groups = (n + kSlotsPerWarp - 1) / kSlotsPerWarp;
+    {
+        int sms = 0, per1 = 0, per2 = 0;
+        CU(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+        CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per1, k_shoot<T, false, true, 3, 4>, kShootThreads, d.shoot_smem()));
+        if constexpr (std::is_same<T, float>::value)
+            CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per2, k_shoot<T, false, true, 4, 1>, kShootThreads,
+                                                             d.shoot_smem()));
+        else
+            per2 = per1;
+        const int want = (n_groups + kShootThreads / 32 - 1) / (kShootThreads / 32);
+        d.n_cta1 = std::max(1, std::min(want, std::max(1, sms * per1)));
+        d.n_cta2 = std::max(1, std::min(want, std::max(1, sms * per2)));
+        // the throughput form once there are over 4 groups per resident warp
+        const long long warps2 = (long long)sms * std::max(per2, 1) * (kShootThreads / 32);
+        d.layout = (std::is_same<T, float>::value && d.P == 1 && n_groups > 4 * warps2) ? 2 : 1;
+        d.n_cta = d.layout == 2 ? d.n_cta2 : d.n_cta1;
+    }
     int *d_heavy, *d_stamp, *d_early, *d_estamp;
     if ((rc = d.alloc(&d.d_shooters, (size_t)d.P)) || (rc = d.alloc(&d.d_state, 1)) ||
-        (rc = d.alloc(&d.d_part, (size_t)d.n_cta)) || (rc = d.alloc(&d_heavy, 2 * (size_t)n_groups)) ||
+        (rc = d.alloc(&d.d_part, (size_t)std::max(d.n_cta1, d.n_cta2))) || (rc = d.alloc(&d_heavy, 2 * (size_t)n_groups)) ||
         (rc = d.alloc(&d_stamp, (size_t)n_groups)) || (rc = d.alloc(&d.d_unshot, (size_t)kUnshotCtas + 1)) ||
         (rc = d.alloc(&d_early, 2 * (size_t)n_groups)) || (rc = d.alloc(&d_estamp, (size_t)n_groups)))
         return rc;
@@ -587,7 +614,7 @@ int upload(const Scene<T>& s, const Octree<T>& o, const rad_options& opt, int de
     st.t_start = ~0ull;
     CU(cudaMemcpyAsync(d.d_state, &st, sizeof st, cudaMemcpyHostToDevice, d.stream));
     CU(cudaMemsetAsync(d.d_shooters, 0, sizeof(Shooter<T>) * d.P, d.stream));
-    CU(cudaMemsetAsync(d.d_part, 0, sizeof(Partial) * d.n_cta, d.stream));
+    CU(cudaMemsetAsync(d.d_part, 0, sizeof(Partial) * std::max(d.n_cta1, d.n_cta2), d.stream));
     // initial selection keys: a step with no shooter only reduces the keys
     launch_shoot(d, d.stream);
     CU(cudaGetLastError());
@@ -602,19 +629,24 @@ int upload(const Scene<T>& s, const Octree<T>& o, const rad_options& opt, int de
 template <typename T>
 void launch_shoot(DevImpl<T>& d, cudaStream_t s) {
     const bool fused = d.P == 1;
+    // counting, several shooters per step and FP64 use the tail-bound form
     if (d.counting && fused)
-        k_shoot<T, true, true><<<d.n_cta, kShootThreads, d.shoot_smem(), s>>>(d.S, d.G, d.d_shooters, d.d_state, d.d_part, d.conv);
+        k_shoot<T, true, true, 3, 4><<<d.n_cta1, kShootThreads, d.shoot_smem(), s>>>(d.S, d.G, d.d_shooters, d.d_state, d.d_part, d.conv);
     else if (d.counting)
-        k_shoot<T, true, false><<<d.n_cta, kShootThreads, d.shoot_smem(), s>>>(d.S, d.G, d.d_shooters, d.d_state, d.d_part, d.conv);
-    else if (fused)
-        k_shoot<T, false, true><<<d.n_cta, kShootThreads, d.shoot_smem(), s>>>(d.S, d.G, d.d_shooters, d.d_state, d.d_part, d.conv);
+        k_shoot<T, true, false, 3, 4><<<d.n_cta1, kShootThreads, d.shoot_smem(), s>>>(d.S, d.G, d.d_shooters, d.d_state, d.d_part, d.conv);
+    else if (fused && d.layout == 2) {
+        if constexpr (std::is_same<T, float>::value)
+            k_shoot<T, false, true, 4, 1><<<d.n_cta2, kShootThreads, d.shoot_smem(), s>>>(d.S, d.G, d.d_shooters, d.d_state,
+                                                                                       d.d_part, d.conv);
+    } else if (fused)
+        k_shoot<T, false, true, 3, 4><<<d.n_cta1, kShootThreads, d.shoot_smem(), s>>>(d.S, d.G, d.d_shooters, d.d_state, d.d_part, d.conv);
     else
-        k_shoot<T, false, false><<<d.n_cta, kShootThreads, d.shoot_smem(), s>>>(d.S, d.G, d.d_shooters, d.d_state, d.d_part, d.conv);
+        k_shoot<T, false, false, 3, 4><<<d.n_cta1, kShootThreads, d.shoot_smem(), s>>>(d.S, d.G, d.d_shooters, d.d_state, d.d_part, d.conv);
 }
 
 template <typename T>
 int launch_step(DevImpl<T>& d, cudaStream_t s) {
-    if (d.P > 1) k_setup<T><<<1, kSetupThreads, 0, s>>>(d.S, d.d_shooters, d.d_state, d.d_part, d.n_cta, d.conv, d.P);
+    if (d.P > 1) k_setup<T><<<1, kSetupThreads, 0, s>>>(d.S, d.d_shooters, d.d_state, d.d_part, d.n_cta1, d.conv, d.P);
     launch_shoot(d, s);
     CU(cudaGetLastError());
     return RAD_OK;
@@ -622,7 +654,7 @@ int launch_step(DevImpl<T>& d, cudaStream_t s) {
 
 template <typename T>
 int graph_for(DevImpl<T>& d, int steps, cudaGraphExec_t* out) {
-    cudaGraphExec_t& slot = d.graphs[d.counting ? 1 : 0][steps];
+    cudaGraphExec_t& slot = d.graphs[d.layout][d.counting ? 1 : 0][steps];
     if (!slot) {
         cudaGraph_t g;
         CU(cudaStreamBeginCapture(d.stream, cudaStreamCaptureModeThreadLocal));
@@ -687,7 +719,7 @@ int run(DevImpl<T>& d, long long max_steps, long long* done_steps, int* converge
         if (mode == 2) {
             // one step per iteration, kernels timed separately
             CU(cudaEventRecord(d.ev[0], d.stream));
-            if (d.P > 1) k_setup<T><<<1, kSetupThreads, 0, d.stream>>>(d.S, d.d_shooters, d.d_state, d.d_part, d.n_cta, d.conv, d.P);
+            if (d.P > 1) k_setup<T><<<1, kSetupThreads, 0, d.stream>>>(d.S, d.d_shooters, d.d_state, d.d_part, d.n_cta1, d.conv, d.P);
             CU(cudaEventRecord(d.ev[1], d.stream));
             launch_shoot(d, d.stream);
             CU(cudaGetLastError());
@@ -984,6 +1016,33 @@ int rad_dev_set_schedule(rad_dev* h, double split_frac, double split_frac_split,
         return RAD_OK;
     };
     return h->d32 ? go(*h->d32) : go(*h->d64);
+}
+
+int rad_dev_set_layout(rad_dev* h, int32_t layout) {
+    if (!h) return fail(RAD_ERR_ARG, "rad_dev_set_layout: null handle");
+    if (layout < 0 || layout > 2) return fail(RAD_ERR_ARG, "rad_dev_set_layout: layout must be 0, 1 or 2");
+    if (h->d32) {
+        DevImpl<float>& d = *h->d32;
+        if (layout == 0) {
+            int sms = 0, per2 = 0;
+            CU(cudaSetDevice(d.device));
+            CU(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, d.device));
+            CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per2, k_shoot<float, false, true, 4, 1>, kShootThreads,
+                                                             d.shoot_smem()));
+            const int n_groups = (d.S.n + kSlotsPerWarp - 1) / kSlotsPerWarp;
+            const long long warps2 = (long long)sms * std::max(per2, 1) * (kShootThreads / 32);
+            layout = (d.P == 1 && n_groups > 4 * warps2) ? 2 : 1;
+        }
+        if (layout == 2 && d.P != 1) layout = 1;
+        d.layout = layout;
+        d.n_cta = layout == 2 ? d.n_cta2 : d.n_cta1;
+    }
+    return RAD_OK;   // the FP64 solver has only the tail-bound form
+}
+
+int rad_dev_layout(const rad_dev* h) {
+    if (!h) return 0;
+    return h->d32 ? h->d32->layout : 1;
 }
 
 int rad_dev_set_counting(rad_dev* h, int32_t on) {

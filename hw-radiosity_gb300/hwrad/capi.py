@@ -25,7 +25,7 @@ EXPORTS = [
     "rad_scene_view_get", "rad_scene_write_fin", "rad_scene_log", "rad_scene_free",
     "rad_octree_build", "rad_octree_info", "rad_octree_cell_coords", "rad_octree_free",
     "rad_dev_create", "rad_dev_run", "rad_dev_run_timed", "rad_dev_run_profiled", "rad_dev_download", "rad_dev_trace", "rad_dev_stats",
-    "rad_dev_set_counting", "rad_dev_set_schedule", "rad_dev_ray_hit", "rad_dev_form_factors", "rad_dev_form_factors_noalloc",
+    "rad_dev_set_counting", "rad_dev_set_schedule", "rad_dev_set_layout", "rad_dev_layout", "rad_dev_ray_hit", "rad_dev_form_factors", "rad_dev_form_factors_noalloc",
     "rad_dev_destroy",
     "rad_batch_create", "rad_batch_run", "rad_batch_run_timed", "rad_batch_scene_stats", "rad_batch_download",
     "rad_batch_trace", "rad_batch_stats", "rad_batch_set_counting", "rad_batch_destroy",
@@ -106,6 +106,8 @@ def load(path: Optional[str] = None) -> C.CDLL:
         "rad_dev_trace": (C.c_int, [vp, vp, i64, P(i64)]),
         "rad_dev_stats": (C.c_int, [vp, P(Stats)]),
         "rad_dev_set_counting": (C.c_int, [vp, i32]),
+        "rad_dev_set_layout": (C.c_int, [vp, i32]),
+        "rad_dev_layout": (C.c_int, [vp]),
         "rad_dev_ray_hit": (C.c_int, [vp, vp, vp, vp, i32, vp]),
         "rad_dev_form_factors": (C.c_int, [vp, i32, vp, i32, vp]),
         "rad_dev_form_factors_noalloc": (C.c_int, [vp, vp, i32, vp, i32, vp, vp]),
@@ -326,6 +328,14 @@ class Device:
         """Limits of the single-shooter schedule (rad_dev_set_schedule); all 0
         splits every group after the first step."""
         _check(load().rad_dev_set_schedule(self.h, split_frac, split_frac_split, split_mean_mult, early_mean_mult))
+
+    def set_layout(self, layout: int = 0):
+        """k_shoot form (rad_dev_set_layout): 0 auto, 1 tail-bound, 2 throughput."""
+        _check(load().rad_dev_set_layout(self.h, int(layout)))
+
+    @property
+    def layout(self) -> int:
+        return int(load().rad_dev_layout(self.h))
 
     def ray_hit(self, p: np.ndarray, v: np.ndarray, ban: np.ndarray, dtype=np.float32) -> np.ndarray:
         p = np.ascontiguousarray(p, dtype).reshape(-1, 3)

@@ -185,6 +185,16 @@ int rad_dev_stats(const rad_dev* d, rad_stats* st);
 int rad_dev_set_schedule(rad_dev* d, double split_frac, double split_frac_split, double split_mean_mult,
                          double early_mean_mult);
 int rad_dev_set_counting(rad_dev* d, int32_t on);
+/* Which k_shoot form the single-shooter FP32 solver launches (no reference
+ * counterpart; results do not depend on it).  1: 3 CTAs per SM, slow groups
+ * split across 4 lanes per corner (for scenes whose step is bound by its
+ * slowest groups).  2: 4 CTAs per SM, slow groups split into 3-slot items on
+ * one lane each (for scenes with over 4 groups per resident warp, bound by
+ * throughput).  0: choose by that rule, as the upload does.  Several shooters
+ * per step, counting and FP64 always use form 1. */
+int rad_dev_set_layout(rad_dev* d, int32_t layout);
+/* The form chosen (1 or 2). */
+int rad_dev_layout(const rad_dev* d);
 /* Batched RayHitted (src/raycast.cpp:335-360): for each i, the triangle the
  * walk from p[i] along v[i] (not normalised) stops at, skipping ban[i]; -1 if
  * it leaves the grid.  Host arrays in and out (precision 32: float). */

@@ -21,7 +21,7 @@ pytestmark = pytest.mark.gpu
 CASES = sorted(k for k, v in golden_index().items() if not v.get("adaptive"))
 
 
-def _solve(tri, argv, fp64=False, chunks=None, schedule=None, **kw):
+def _solve(tri, argv, fp64=False, chunks=None, schedule=None, layout=None, **kw):
     o = capi.options_from_argv(argv, precision=64 if fp64 else 32, **kw)
     sc = capi.Scene.load(tri, o)
     tree = capi.Octree(sc, 4)
@@ -30,6 +30,8 @@ def _solve(tri, argv, fp64=False, chunks=None, schedule=None, **kw):
     dv = capi.Device(sc, tree, o)
     if schedule is not None:
         dv.set_schedule(*schedule)
+    if layout is not None:
+        dv.set_layout(layout)
     if chunks:
         total = 0
         for c in chunks:
@@ -249,6 +251,7 @@ def test_hall_bounded_steps_equal_oracle(built, workdir):
     sc.init()
     sc.prepartition()
     dv = capi.Device(sc, tree, o)
+    assert dv.layout == 2   # over 4 groups per resident warp: the throughput form
     n, conv, _ = dv.run(steps)
     assert n == steps
     dv.download(sc)
@@ -299,13 +302,19 @@ SPLIT_NEVER = (1e9, 1e9, 1e9, 1e9)
 
 @pytest.mark.parametrize("name", [c for c in CASES if not golden_index()[c].get("P", 1) > 1])
 @pytest.mark.parametrize("schedule", [SPLIT_ALWAYS, SPLIT_NEVER], ids=["split_always", "split_never"])
-def test_schedule_does_not_change_results(built, workdir, name, schedule):
-    """The schedule (which groups are split into 4-lane items, which start
-    early) changes only timing: with every group split from the second step
-    on (the 4-lane walk and its NaN fallback everywhere, FP32 and FP64) and
-    with nothing split, the results equal the reference fixture bit for bit."""
+@pytest.mark.parametrize("layout", [1, 2])
+def test_schedule_does_not_change_results(built, workdir, name, schedule, layout):
+    """The schedule (which groups are split, which start early) and the
+    kernel form change only timing.  Form 1 splits a group into 2-slot items
+    with 4 lanes per corner, form 2 into 3-slot items on one lane.  With every
+    group split from the second step on (in form 1 the 4-lane walk and its NaN
+    fallback everywhere, FP32 and FP64) and with nothing split, the results
+    equal the reference fixture bit for bit."""
     tri, argv, idx = write_case(name, workdir)
-    sc, dv, steps, conv = _solve(tri, argv, fp64=idx["fp64"], schedule=schedule)
+    if layout == 2 and idx["fp64"]:
+        pytest.skip("the FP64 solver has only form 1")
+    sc, dv, steps, conv = _solve(tri, argv, fp64=idx["fp64"], schedule=schedule, layout=layout)
+    assert dv.layout == layout
     g = golden(name)
     assert conv
     assert steps == idx["steps"]
@@ -316,13 +325,14 @@ def test_schedule_does_not_change_results(built, workdir, name, schedule):
 
 
 def test_split_schedule_on_hall_steps(built, workdir):
-    """The 422k-triangle hall with every group split, 40 steps: equal to the
-    same steps with nothing split (the unsplit path is held to the oracle by
+    """The 422k-triangle hall, 40 steps, in both kernel forms with every group
+    split and with nothing split: all four runs equal (the first steps of the
+    automatic choice are held to the oracle by
     test_hall_bounded_steps_equal_oracle)."""
     sc_gen = scenes.hall()
     tri = sc_gen.write(os.path.join(workdir, "hall_split.tri"))
     out = []
-    for sched in (SPLIT_ALWAYS, SPLIT_NEVER):
+    for layout, sched in ((1, SPLIT_ALWAYS), (1, SPLIT_NEVER), (2, SPLIT_ALWAYS), (2, SPLIT_NEVER)):
         o = capi.options_from_argv(sc_gen.argv())
         sc = capi.Scene.load(tri, o)
         tree = capi.Octree(sc, 8)
@@ -330,11 +340,46 @@ def test_split_schedule_on_hall_steps(built, workdir):
         sc.prepartition()
         dv = capi.Device(sc, tree, o)
         dv.set_schedule(*sched)
+        dv.set_layout(layout)
+        assert dv.layout == layout
         dv.run(40)
         dv.download(sc)
         v = sc.view()
         out.append((dv.trace().copy(), v["accB"].copy(), v["deltaB"].copy()))
         dv.close()
-    assert np.array_equal(out[0][0], out[1][0])
-    assert same_bits(out[0][1], out[1][1])
-    assert same_bits(out[0][2], out[1][2])
+    for o in out[1:]:
+        assert np.array_equal(out[0][0], o[0])
+        assert same_bits(out[0][1], o[1])
+        assert same_bits(out[0][2], o[2])
+
+
+def test_layout_choice(built, workdir):
+    """The automatic form: 1 for a scene with few groups per resident warp,
+    2 above 4 (FP32, one shooter per step); several shooters per step and FP64
+    stay in form 1 whatever is asked."""
+    tri, argv, idx = write_case("room8", workdir)
+    o = capi.options_from_argv(argv)
+    sc = capi.Scene.load(tri, o)
+    tree = capi.Octree(sc, 4)
+    sc.init()
+    sc.prepartition()
+    dv = capi.Device(sc, tree, o)
+    assert dv.layout == 1
+    dv.set_layout(2)
+    assert dv.layout == 2
+    dv.set_layout(0)
+    assert dv.layout == 1
+    with pytest.raises(capi.RadError):
+        dv.set_layout(3)
+    dv.close()
+    for name in ("room8_p3", "room8_fp64"):
+        tri, argv, idx = write_case(name, workdir)
+        o = capi.options_from_argv(argv, precision=64 if idx["fp64"] else 32)
+        sc = capi.Scene.load(tri, o)
+        tree = capi.Octree(sc, 4)
+        sc.init()
+        sc.prepartition()
+        dv = capi.Device(sc, tree, o)
+        dv.set_layout(2)
+        assert dv.layout == 1, name
+        dv.close()
