@@ -44,13 +44,13 @@ namespace radgb {
 namespace dev {
 
 // Persistent: each warp takes 10-slot groups from the step's queue until it
-// is empty, so warps that finish early take more work; the CTA's (key, slot)
-// maximum is written by whichever of its warps finishes last.
+// is empty, so warps that finish early take more work; once all its warps are
+// done, thread 0 writes the CTA's (key, slot) maximum.
 //
-// FUSED (one shooter per step): the last warp of the whole grid to finish
-// also does the next step's selection -- it reduces the per-CTA partials,
-// builds the next shooter record and advances the step -- so a step is one
-// kernel.  Several shooters per step keep the separate k_setup.
+// FUSED (one shooter per step): the last CTA of the grid to finish also does
+// the next step's selection -- it reduces the per-CTA partials, builds the
+// next shooter record and advances the step -- so a step is one kernel.
+// Several shooters per step keep the separate k_setup.
 // a group is split in the next step when its item took longer than this
 // fraction of the step (an item that was already split: the second figure)
 #ifndef RAD_HEAVY_FRAC
@@ -75,8 +75,8 @@ namespace dev {
 //   2 (throughput-bound: many groups per warp, e.g. 400k triangles) -- 4 CTAs
 //     per SM, 64 registers, split items keep one lane per corner (3 slots
 //     per item) so the walk is inlined once and more warps hide latency.
-// Measured: the 61k-triangle room 9.7k vs 7.7k shots/s (flushed) in form 1
-// vs 2; the 422k-triangle hall 841 vs 998 shots/s.
+// Measured: the 61k-triangle room 9.4k vs 7.7k shots/s (flushed) in form 1
+// vs 2; the 422k-triangle hall 813 vs 997 shots/s.
 template <int HL>
 __host__ __device__ constexpr int heavy_slots() { return HL == 1 ? 3 : 32 / (3 * HL); }
 template <int HL>
