@@ -63,3 +63,31 @@ def build_fp_forms_check(workdir):
                     "-I", os.path.join(repo, "hw-radiosity_gb300", "csrc"), "-I", os.path.join(repo, "include"),
                     "-o", exe, os.path.join(here, "fp_forms_check.cu")], check=True, capture_output=True)
     return exe
+
+
+EDGE_SCENES = ["empty", "dark", "one", "two"]
+
+
+def write_edge_scene(name, workdir):
+    """Small edge inputs: an empty file, a room with no emitter, one emitting
+    triangle, and an emitting triangle with one receiver.  Returns
+    (tri_path, argv)."""
+    from hwrad import scenes
+    path = os.path.join(workdir, f"edge_{name}.tri")
+    if name == "empty":
+        open(path, "w").close()
+        return path, []
+    if name == "dark":
+        s = scenes.room(4, emitter=(0.0, 0.0), name="dark")
+    elif name == "one":
+        s = scenes.Scene(vtx=np.array([[[0, 0, 0], [1, 0, 0], [0, 1, 0]]], np.float32),
+                         frgb=np.array([[100, 100, 100]]), brgb=np.array([[255, 255, 255]]),
+                         options={"-light": "0.05"}, name="one")
+    elif name == "two":
+        s = scenes.Scene(vtx=np.array([[[0, 0, 0], [0, 1, 0], [1, 0, 0]], [[0, 0, 2], [1, 0, 2], [0, 1, 2]]],
+                                      np.float32),
+                         frgb=np.array([[100, 100, 100], [200, 150, 100]]),
+                         brgb=np.array([[255, 255, 255], [0, 0, 0]]), options={"-light": "0.05"}, name="two")
+    else:
+        raise ValueError(name)
+    return s.write(path), s.argv()

@@ -7,7 +7,7 @@ import numpy as np
 import pytest
 
 import runner
-from helpers import same_bits
+from helpers import EDGE_SCENES, same_bits, write_edge_scene
 from hwrad import scenes
 
 REF_MODELS = "/root/reference/model"
@@ -44,3 +44,18 @@ def test_oracle_counters_equal_reference(built, workdir):
     ca, cb = runner.counters(a["stderr"]), runner.counters(b["stderr"])
     assert cb.pop("loops") == 0          # no walk of this scene repeats a state
     assert ca == cb
+
+
+@pytest.mark.skipif(not runner.have_ref(), reason="reference binary not built here")
+@pytest.mark.parametrize("name", EDGE_SCENES)
+@pytest.mark.parametrize("fp64", [False, True])
+@pytest.mark.parametrize("P", [1, 2])
+def test_oracle_equals_reference_on_edge_scenes(built, workdir, name, fp64, P):
+    tri, argv = write_edge_scene(name, workdir)
+    argv = argv + ["-parallel_src", str(P)]
+    a = runner.run(runner.REF64 if fp64 else runner.REF32, tri, argv + ["-jobs", "2"])
+    b = runner.oracle(tri, argv, fp64=fp64)
+    assert a["trace"] == b["trace"]
+    for k in ("parent", "p", "accB", "deltaB"):
+        assert same_bits(a["dump"][k], b["dump"][k]), k
+    assert a["fin"] == b["fin"]
