@@ -485,6 +485,7 @@ struct DevImpl : DevBase {
     long long trace_cap = 0;
     int n_cta = 0;          // CTAs of the current layout's kernel
     int n_cta1 = 0, n_cta2 = 0;
+    int n_cta_of(int l) const { return l == 2 ? n_cta2 : n_cta1; }
     int layout = 1;         // 1 tail-bound form, 2 throughput form (FP32, one shooter per step)
     int P = 1;
     T conv = 0;
@@ -583,7 +584,7 @@ int upload(const Scene<T>& s, const Octree<T>& o, const rad_options& opt, int de
         // the throughput form once there are over 4 groups per resident warp
         const long long warps2 = (long long)sms * std::max(per2, 1) * (kShootThreads / 32);
         d.layout = (std::is_same<T, float>::value && d.P == 1 && n_groups > 4 * warps2) ? 2 : 1;
-        d.n_cta = d.layout == 2 ? d.n_cta2 : d.n_cta1;
+        d.n_cta = d.n_cta_of(d.layout);
     }
     int *d_heavy, *d_stamp, *d_early, *d_estamp;
     if ((rc = d.alloc(&d.d_shooters, (size_t)d.P)) || (rc = d.alloc(&d.d_state, 1)) ||
@@ -1018,6 +1019,66 @@ int rad_dev_set_schedule(rad_dev* h, double split_frac, double split_frac_split,
     return h->d32 ? go(*h->d32) : go(*h->d64);
 }
 
+int rad_dev_autotune(rad_dev* h, int32_t steps_per_trial, int64_t max_steps, int64_t* steps_done,
+                     int32_t* converged, int32_t* chosen) {
+    if (!h) return fail(RAD_ERR_ARG, "rad_dev_autotune: null handle");
+    if (steps_per_trial < 1 || steps_per_trial > 32) return fail(RAD_ERR_ARG, "rad_dev_autotune: steps_per_trial must be 1..32");
+    long long total = 0;
+    int cv = 0, walk_rc = RAD_OK;
+    // a capped walk (RAD_ERR_WALK) is reported at the end, as rad_dev_run does
+    auto go_run = [&](auto& d, long long n, double* ms) -> int {
+        long long sd = 0;
+        int c = 0;
+        int rc = run(d, n, &sd, &c, ms ? 1 : 0, ms, nullptr);
+        total += sd;
+        if (c) cv = 1;
+        if (rc == RAD_ERR_WALK) {
+            walk_rc = rc;
+            rc = RAD_OK;
+        }
+        return rc;
+    };
+    if (h->d32 && h->d32->P == 1 && !h->d32->counting) {
+        DevImpl<float>& d = *h->d32;
+        const int before = d.layout;
+        // one untimed step per form (first launches), then trials of both
+        // forms in alternating order until max_steps is used up
+        double ms[3] = {0, 0, 0};
+        long long n[3] = {0, 0, 0};
+        for (int r = 0; !cv && total < max_steps; r++) {
+            for (int k = 0; k < 2 && !cv && total < max_steps; k++) {
+                const int layout = ((r + k) & 1) ? 2 : 1;
+                d.layout = layout;
+                d.n_cta = d.n_cta_of(layout);
+                if (r == 0) {
+                    int rc = go_run(d, 1, nullptr);
+                    if (rc) return rc;
+                    continue;
+                }
+                const long long want = std::min<long long>(steps_per_trial, max_steps - total);
+                const long long had = total;
+                double t = 0;
+                int rc = go_run(d, want, &t);
+                if (rc) return rc;
+                ms[layout] += t;
+                n[layout] += total - had;
+            }
+        }
+        int best = before;
+        if (n[1] > 0 && n[2] > 0) best = ms[2] / (double)n[2] < ms[1] / (double)n[1] ? 2 : 1;
+        d.layout = best;
+        d.n_cta = d.n_cta_of(best);
+    } else if (max_steps > 0) {
+        // one form only: the steps run as rad_dev_run would run them
+        int rc = h->d32 ? go_run(*h->d32, max_steps, nullptr) : go_run(*h->d64, max_steps, nullptr);
+        if (rc) return rc;
+    }
+    if (steps_done) *steps_done = total;
+    if (converged) *converged = cv;
+    if (chosen) *chosen = h->d32 ? h->d32->layout : 1;
+    return walk_rc;
+}
+
 int rad_dev_set_layout(rad_dev* h, int32_t layout) {
     if (!h) return fail(RAD_ERR_ARG, "rad_dev_set_layout: null handle");
     if (layout < 0 || layout > 2) return fail(RAD_ERR_ARG, "rad_dev_set_layout: layout must be 0, 1 or 2");
@@ -1035,7 +1096,7 @@ int rad_dev_set_layout(rad_dev* h, int32_t layout) {
         }
         if (layout == 2 && d.P != 1) layout = 1;
         d.layout = layout;
-        d.n_cta = layout == 2 ? d.n_cta2 : d.n_cta1;
+        d.n_cta = d.n_cta_of(layout);
     }
     return RAD_OK;   // the FP64 solver has only the tail-bound form
 }

@@ -61,6 +61,8 @@ void usage(const char* argv0, const rad_options& o) {
     fprintf(stderr, "   GPU Options (extensions)\n");
     fprintf(stderr, "       -device <integer>       CUDA device (default 0)\n");
     fprintf(stderr, "       -fp64                   All-FP64 solver (the reference's float->double build)\n");
+    fprintf(stderr, "       -autotune               Time both forms of the shooting kernel on the first loops\n");
+    fprintf(stderr, "                               and keep the faster (results are the same either way)\n");
     fprintf(stderr, "       -adaptive               Adaptive split variant (config.h = ADAPT + ROLLBACK: serial\n");
     fprintf(stderr, "                               loop, delta-FF split test, no pre-partition)\n");
     fprintf(stderr, "   Headless render of the result (the WebGL viewer's initial view, CUDA rasteriser)\n");
@@ -218,6 +220,7 @@ int main(int argc, char* argv[]) {
     rad_render_options_default(&g_ro);
     int device = 0;
     bool adaptive = false;
+    bool autotune = false;
     if (argc < 3) {
         usage(argv[0], o);
         return 1;
@@ -243,7 +246,7 @@ int main(int argc, char* argv[]) {
     }
     static const char* opts[] = {"-debug", "-adapt_area", "-sample_area", "-converge", "-delta_ff",
                                  "-write_cycle", "-zip", "-triangle", "-light", "-o", "-interactive",
-                                 "-jobs", "-parallel_src", "-device", "-fp64", "-adaptive"};
+                                 "-jobs", "-parallel_src", "-device", "-fp64", "-adaptive", "-autotune"};
     const int n_opts = (int)(sizeof opts / sizeof opts[0]);
     const char* in = nullptr;
     const char* out = "./test";
@@ -279,6 +282,7 @@ int main(int argc, char* argv[]) {
             case 13: geti(device, "Device Error"); break;
             case 14: o.precision = 64; break;
             case 15: adaptive = true; break;
+            case 16: autotune = true; break;
         }
     }
     fprintf(stderr, "[" KGRN "INFO" KWHT "] Input Model " KMAG "%s" KWHT " and Output Prefix " KMAG "%s\n" KWHT,
@@ -322,7 +326,16 @@ int main(int argc, char* argv[]) {
         long long target = W > 0 ? ((loop + W - 1) / W) * W : loop + (1LL << 40);
         int64_t done = 0;
         int32_t conv = 0;
-        int rc = rad_dev_run(dev, target - loop + 1, &done, &conv);
+        int rc;
+        if (autotune && loop == 1) {
+            int32_t form = 0;
+            rc = rad_dev_autotune(dev, 8, std::min<long long>(target - loop + 1, 64), &done, &conv, &form);
+            if (rc == RAD_OK || rc == RAD_ERR_WALK)
+                fprintf(stderr, "[" KGRN "INFO" KWHT "] Shooting kernel form %d, autotuned over %lld loops\n", form,
+                        (long long)done);
+        } else {
+            rc = rad_dev_run(dev, target - loop + 1, &done, &conv);
+        }
         if (rc == RAD_ERR_WALK) fprintf(stderr, "[" KRED "WARN" KWHT "] %s\n", rad_last_error());
         else check(rc, "shooting loop");
         long long last = loop + done - 1;   // last loop that shot

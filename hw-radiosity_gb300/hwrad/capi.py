@@ -25,7 +25,7 @@ EXPORTS = [
     "rad_scene_view_get", "rad_scene_write_fin", "rad_scene_log", "rad_scene_free",
     "rad_octree_build", "rad_octree_info", "rad_octree_cell_coords", "rad_octree_free",
     "rad_dev_create", "rad_dev_run", "rad_dev_run_timed", "rad_dev_run_profiled", "rad_dev_download", "rad_dev_trace", "rad_dev_stats",
-    "rad_dev_set_counting", "rad_dev_set_schedule", "rad_dev_set_layout", "rad_dev_layout", "rad_dev_ray_hit", "rad_dev_form_factors", "rad_dev_form_factors_noalloc",
+    "rad_dev_set_counting", "rad_dev_set_schedule", "rad_dev_set_layout", "rad_dev_layout", "rad_dev_autotune", "rad_dev_ray_hit", "rad_dev_form_factors", "rad_dev_form_factors_noalloc",
     "rad_dev_destroy",
     "rad_batch_create", "rad_batch_run", "rad_batch_run_timed", "rad_batch_scene_stats", "rad_batch_download",
     "rad_batch_trace", "rad_batch_stats", "rad_batch_set_counting", "rad_batch_destroy",
@@ -108,6 +108,7 @@ def load(path: Optional[str] = None) -> C.CDLL:
         "rad_dev_set_counting": (C.c_int, [vp, i32]),
         "rad_dev_set_layout": (C.c_int, [vp, i32]),
         "rad_dev_layout": (C.c_int, [vp]),
+        "rad_dev_autotune": (C.c_int, [vp, i32, i64, C.POINTER(i64), C.POINTER(i32), C.POINTER(i32)]),
         "rad_dev_ray_hit": (C.c_int, [vp, vp, vp, vp, i32, vp]),
         "rad_dev_form_factors": (C.c_int, [vp, i32, vp, i32, vp]),
         "rad_dev_form_factors_noalloc": (C.c_int, [vp, vp, i32, vp, i32, vp, vp]),
@@ -336,6 +337,14 @@ class Device:
     @property
     def layout(self) -> int:
         return int(load().rad_dev_layout(self.h))
+
+    def autotune(self, steps_per_trial: int = 8, max_steps: int = 64):
+        """Time both k_shoot forms on this scene's own steps and keep the
+        faster (rad_dev_autotune); returns (steps shot, converged, form)."""
+        n, cv, ch = C.c_int64(), C.c_int32(), C.c_int32()
+        _check(load().rad_dev_autotune(self.h, int(steps_per_trial), int(max_steps), C.byref(n), C.byref(cv),
+                                       C.byref(ch)), allow=(RAD_ERR_WALK,))
+        return int(n.value), bool(cv.value), int(ch.value)
 
     def ray_hit(self, p: np.ndarray, v: np.ndarray, ban: np.ndarray, dtype=np.float32) -> np.ndarray:
         p = np.ascontiguousarray(p, dtype).reshape(-1, 3)

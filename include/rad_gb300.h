@@ -195,6 +195,15 @@ int rad_dev_set_counting(rad_dev* d, int32_t on);
 int rad_dev_set_layout(rad_dev* d, int32_t layout);
 /* The form chosen (1 or 2). */
 int rad_dev_layout(const rad_dev* d);
+/* Choose the form by timing both on this scene's own steps: one untimed step
+ * in each form, then trials of steps_per_trial (1..32) steps in each form, in
+ * alternating order, until max_steps steps have been shot or the solution
+ * converged.  The faster form per step is kept (*chosen).  The steps are
+ * ordinary solver steps (counted in *steps_done, traced, results unchanged);
+ * a handle with one form (FP64, several shooters per step, counting) just
+ * runs them. */
+int rad_dev_autotune(rad_dev* d, int32_t steps_per_trial, int64_t max_steps, int64_t* steps_done,
+                     int32_t* converged, int32_t* chosen);
 /* Batched RayHitted (src/raycast.cpp:335-360): for each i, the triangle the
  * walk from p[i] along v[i] (not normalised) stops at, skipping ban[i]; -1 if
  * it leaves the grid.  Host arrays in and out (precision 32: float). */

@@ -207,12 +207,15 @@ def test_walk_cap_reports_error(built, workdir):
     assert dv.stats()["walk_cap_hits"] > 0
 
 
-def test_cli_outputs_equal_oracle(built, workdir):
+@pytest.mark.parametrize("autotune", [False, True])
+def test_cli_outputs_equal_oracle(built, workdir, autotune):
     tri, argv, idx = write_case("room8", workdir)
-    prefix = os.path.join(workdir, "cli_room8")
-    r = subprocess.run([build.BIN, tri] + argv + ["-write_cycle", "250", "-o", prefix],
+    prefix = os.path.join(workdir, f"cli_room8_{int(autotune)}")
+    r = subprocess.run([build.BIN, tri] + argv + ["-write_cycle", "250", "-o", prefix] + (["-autotune"] if autotune else []),
                        capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stderr
+    if autotune:
+        assert "autotuned over 64 loops" in r.stderr
     assert "Complete in #Iterations 744" in r.stderr
     with open(prefix + ".fin", "rb") as fh:
         assert hashlib.sha256(fh.read()).hexdigest() == idx["fin_sha256"]
@@ -332,17 +335,21 @@ def test_split_schedule_on_hall_steps(built, workdir):
     sc_gen = scenes.hall()
     tri = sc_gen.write(os.path.join(workdir, "hall_split.tri"))
     out = []
-    for layout, sched in ((1, SPLIT_ALWAYS), (1, SPLIT_NEVER), (2, SPLIT_ALWAYS), (2, SPLIT_NEVER)):
+    for layout, sched in ((1, SPLIT_ALWAYS), (1, SPLIT_NEVER), (2, SPLIT_ALWAYS), (2, SPLIT_NEVER), (0, None)):
         o = capi.options_from_argv(sc_gen.argv())
         sc = capi.Scene.load(tri, o)
         tree = capi.Octree(sc, 8)
         sc.init()
         sc.prepartition()
         dv = capi.Device(sc, tree, o)
-        dv.set_schedule(*sched)
-        dv.set_layout(layout)
-        assert dv.layout == layout
-        dv.run(40)
+        if layout:
+            dv.set_schedule(*sched)
+            dv.set_layout(layout)
+            assert dv.layout == layout
+            dv.run(40)
+        else:   # both forms timed on the scene's own steps, then the faster kept
+            n, conv, form = dv.autotune(8, 40)
+            assert n == 40 and not conv and form in (1, 2)
         dv.download(sc)
         v = sc.view()
         out.append((dv.trace().copy(), v["accB"].copy(), v["deltaB"].copy()))
@@ -383,3 +390,34 @@ def test_layout_choice(built, workdir):
         dv.set_layout(2)
         assert dv.layout == 1, name
         dv.close()
+
+
+@pytest.mark.parametrize("name", ["room8", "bigroom", "room8_fp64", "room8_p3"])
+def test_autotune_does_not_change_results(built, workdir, name):
+    """rad_dev_autotune shoots ordinary steps in both forms and keeps the
+    faster; the solution equals the reference fixture bit for bit.  FP64 and
+    several shooters per step have one form: the steps just run."""
+    tri, argv, idx = write_case(name, workdir)
+    o = capi.options_from_argv(argv, precision=64 if idx["fp64"] else 32)
+    sc = capi.Scene.load(tri, o)
+    tree = capi.Octree(sc, 4)
+    sc.init()
+    sc.prepartition()
+    dv = capi.Device(sc, tree, o)
+    n, conv, form = dv.autotune(4, 50)
+    assert n == 50 and not conv
+    assert form == dv.layout
+    if idx["fp64"] or idx.get("P", 1) > 1:
+        assert form == 1
+    else:
+        assert form in (1, 2)
+    m, conv, _ = dv.run()
+    assert conv and n + m == idx["steps"]
+    dv.download(sc)
+    g = golden(name)
+    assert np.array_equal(dv.trace(), g["trace"])
+    v = sc.view()
+    for k in ("parent", "p", "accB", "deltaB", "nb"):
+        assert same_bits(v[k], g[k]), k
+    with pytest.raises(capi.RadError):
+        dv.autotune(0, 10)
