@@ -376,6 +376,38 @@ __global__ void k_unshot_total(const double* part, int n, double* out) {
     if (threadIdx.x == 0) *out = t;
 }
 
+// ------------------------------------------------------------------ upload
+// The cell table and the list records are expanded on the device from
+// compact host arrays: a leaf index per cell, and per triangle one record
+// group gathered for each list entry naming it.  The records are the ones
+// pack_scene writes (the batched form still packs on the host).
+template <typename T>
+__global__ void k_expand_cells(const int32_t* __restrict__ cell_leaf, const T* __restrict__ leaf_box,
+                               const int32_t* __restrict__ leaf_range, long long n_cell, CellRec<T>* __restrict__ out) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n_cell;
+         i += (long long)gridDim.x * blockDim.x) {
+        const int l = cell_leaf[i];
+        const T* b = leaf_box + (size_t)l * 8;
+        CellRec<T> r;
+        r.h = make_int4(l, leaf_range[2 * l], leaf_range[2 * l + 1], 0);
+        r.a = {b[0], b[1], b[2], b[4]};
+        r.b = {b[5], b[6], 0, 0};
+        out[i] = r;
+    }
+}
+
+// entry k = the five records of triangle entry_tri[k]
+template <typename T>
+__global__ void k_gather_entries(const int32_t* __restrict__ entry_tri, const Q4<T>* __restrict__ tri_rec,
+                                 long long n_ent, Q4<T>* __restrict__ out) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n_ent * 5;
+         i += (long long)gridDim.x * blockDim.x) {
+        const long long k = i / 5;
+        const int j = (int)(i - 5 * k);
+        out[i] = tri_rec[(size_t)entry_tri[k] * 5 + j];
+    }
+}
+
 // ------------------------------------------------------------------ queries
 template <typename T>
 __global__ void k_ray_hit(Grid<T> G, const T* __restrict__ p, const T* __restrict__ v, const int* __restrict__ ban,
@@ -533,11 +565,36 @@ int upload(const Scene<T>& s, const Octree<T>& o, const rad_options& opt, int de
     const int n = s.trinum;
     if (n < 0) return fail(RAD_ERR_ARG, "negative slot count");
     if (!thresholds_consistent(o)) return fail(RAD_ERR_ARG, "octree cell thresholds do not match its dimensions");
-    HostPack<T> P;
-    pack_scene(s, o, P);
-    Q4<T> *d_vtx, *d_nrm, *d_ctr, *d_frgb, *d_acc, *d_db, *d_ent;
+    // per-slot records, written in place (no per-element growth)
+    std::vector<Q4<T>> h_vtx((size_t)n * 3), h_acc((size_t)n * 3), h_nrm(n), h_ctr(n), h_frgb(n), h_db(n);
+    for (int i = 0; i < n; i++) {
+        const Slot<T>& t = s.slots[i];
+        for (int v = 0; v < 3; v++) {
+            h_vtx[(size_t)i * 3 + v] = {t.p[v][0], t.p[v][1], t.p[v][2], 0};
+            h_acc[(size_t)i * 3 + v] = {t.accB[v][0], t.accB[v][1], t.accB[v][2], 0};
+        }
+        const T nl = (T)std::sqrt(t.n[0] * t.n[0] + t.n[1] * t.n[1] + t.n[2] * t.n[2]);
+        h_nrm[i] = {t.n[0], t.n[1], t.n[2], nl};
+        h_ctr[i] = {t.c[0], t.c[1], t.c[2], t.area};
+        h_frgb[i] = {(T)t.Frgb[0], (T)t.Frgb[1], (T)t.Frgb[2], (T)t.parent};
+        h_db[i] = {t.deltaB[0], t.deltaB[1], t.deltaB[2], 0};
+    }
+    // the walk's triangle records, one group of five per triangle a list names
+    int n_tri = 0;
+    for (int32_t id : o.entry_tri) n_tri = std::max(n_tri, id + 1);
+    if (n_tri > n) return fail(RAD_ERR_ARG, "octree names a triangle beyond the scene");
+    std::vector<Q4<T>> h_trec((size_t)n_tri * 5);
+    for (int id = 0; id < n_tri; id++) {
+        const Slot<T>& t = s.slots[id];
+        Q4<T>* r = &h_trec[(size_t)id * 5];
+        r[0] = {t.n[0], t.n[1], t.n[2], pack_int<T>(id)};
+        r[1] = {t.c[0], t.c[1], t.c[2], 0};
+        for (int e = 0; e < 3; e++) r[2 + e] = {t.se[e][0], t.se[e][1], t.se[e][2], t.se[e][3]};
+    }
+    Q4<T> *d_vtx, *d_nrm, *d_ctr, *d_frgb, *d_acc, *d_db, *d_ent, *d_trec;
     CellRec<T>* d_cell;
-    T* d_thr;
+    T *d_thr, *d_lbox;
+    int32_t *d_cleaf, *d_lrange, *d_etri;
     int rc;
     auto put = [&](auto** dst, const auto& src) -> int {
         int r = d.alloc(dst, src.size());
@@ -545,11 +602,20 @@ int upload(const Scene<T>& s, const Octree<T>& o, const rad_options& opt, int de
         CU(cudaMemcpyAsync(*dst, src.data(), src.size() * sizeof(src[0]), cudaMemcpyHostToDevice, d.stream));
         return RAD_OK;
     };
-    if ((rc = put(&d_vtx, P.vtx)) || (rc = put(&d_nrm, P.nrm)) || (rc = put(&d_ctr, P.ctr)) ||
-        (rc = put(&d_frgb, P.frgb)) || (rc = put(&d_acc, P.acc)) || (rc = put(&d_db, P.db)) ||
-        (rc = put(&d_ent, P.ent)) || (rc = put(&d_cell, P.cell)) ||
-        (rc = put(&d_thr, P.thr)))
+    const long long n_cell = (long long)o.cell_leaf.size(), n_ent = (long long)o.entry_tri.size();
+    if ((rc = put(&d_vtx, h_vtx)) || (rc = put(&d_nrm, h_nrm)) || (rc = put(&d_ctr, h_ctr)) ||
+        (rc = put(&d_frgb, h_frgb)) || (rc = put(&d_acc, h_acc)) || (rc = put(&d_db, h_db)) ||
+        (rc = put(&d_thr, o.thr)) || (rc = put(&d_cleaf, o.cell_leaf)) || (rc = put(&d_lbox, o.leaf_box)) ||
+        (rc = put(&d_lrange, o.leaf_range)) || (rc = put(&d_etri, o.entry_tri)) || (rc = put(&d_trec, h_trec)) ||
+        (rc = d.alloc(&d_cell, (size_t)n_cell)) || (rc = d.alloc(&d_ent, (size_t)n_ent * 5)))
         return rc;
+    if (n_cell > 0)
+        k_expand_cells<T><<<(int)std::min<long long>((n_cell + 255) / 256, 4096), 256, 0, d.stream>>>(
+            d_cleaf, d_lbox, d_lrange, n_cell, d_cell);
+    if (n_ent > 0)
+        k_gather_entries<T><<<(int)std::min<long long>((n_ent * 5 + 255) / 256, 4096), 256, 0, d.stream>>>(
+            d_etri, d_trec, n_ent, d_ent);
+    CU(cudaGetLastError());
     d.S = Slots<T>{n, d_vtx, d_nrm, d_ctr, d_frgb, d_acc, d_db};
     Grid<T> G = grid_params(o, opt.walk_cap);
     G.thr = d_thr;
