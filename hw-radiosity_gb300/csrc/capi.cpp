@@ -198,6 +198,20 @@ int rad_octree_build(const rad_scene* h, int32_t threads, rad_octree** out) {
     return RAD_OK;
 }
 
+int rad_octree_tables(const rad_octree* t, int32_t* cell_leaf, void* leaf_box, int32_t* leaf_range,
+                      int32_t* entry_tri) {
+    if (!t) return fail(RAD_ERR_ARG, "rad_octree_tables: null octree");
+    auto copy = [&](auto& o) {
+        using T = typename std::decay<decltype(o.leaf_box)>::type::value_type;
+        if (cell_leaf) std::memcpy(cell_leaf, o.cell_leaf.data(), o.cell_leaf.size() * 4);
+        if (leaf_box) std::memcpy(leaf_box, o.leaf_box.data(), o.leaf_box.size() * sizeof(T));
+        if (leaf_range) std::memcpy(leaf_range, o.leaf_range.data(), o.leaf_range.size() * 4);
+        if (entry_tri) std::memcpy(entry_tri, o.entry_tri.data(), o.entry_tri.size() * 4);
+    };
+    if (t->precision == 32) copy(t->o32); else copy(t->o64);
+    return RAD_OK;
+}
+
 int rad_octree_info(const rad_octree* t, int64_t* ref_nodes, int64_t* ref_list, int32_t* n_leaves,
                     int64_t* n_entries, int32_t dims[3]) {
     if (!t) return fail(RAD_ERR_ARG, "rad_octree_info: null octree");

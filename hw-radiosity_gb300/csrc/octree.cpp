@@ -21,65 +21,14 @@
 #include <future>
 #include <thread>
 
+#include "octree_build.h"
+#include "octree_geom.h"
 #include "rad_host.h"
 
 namespace radgb {
 namespace {
 
-template <typename T>
-struct Box { T g0[3], g1[3]; };
 
-// segment p0-p1 against the rectangle [g0,g1] in dims (x, y), raycast.cpp:24-60
-template <typename T>
-bool segment_meets_rect(const T* p0, const T* p1, const T* g0, const T* g1, int x, int y) {
-    const unsigned o0 = (p0[x] < g0[x]) | (p0[x] > g1[x]) << 1 | (p0[y] < g0[y]) << 2 | (p0[y] > g1[y]) << 3;
-    const unsigned o1 = (p1[x] < g0[x]) | (p1[x] > g1[x]) << 1 | (p1[y] < g0[y]) << 2 | (p1[y] > g1[y]) << 3;
-    if (o0 & o1) return false;
-    if (!(o0 | o1)) return true;
-    const T a = p1[y] - p0[y], b = p1[x] - p0[x];
-    const T c00 = a * (g0[x] - p0[x]) - b * (g0[y] - p0[y]);
-    if (c00 == 0) return true;
-    const bool neg = c00 < 0;
-    // the line misses the rectangle iff all four corners lie strictly on one side
-    if ((a * (g0[x] - p0[x]) - b * (g1[y] - p0[y]) < 0) != neg) return true;
-    if ((a * (g1[x] - p0[x]) - b * (g0[y] - p0[y]) < 0) != neg) return true;
-    if ((a * (g1[x] - p0[x]) - b * (g1[y] - p0[y]) < 0) != neg) return true;
-    return false;
-}
-
-// point on segment hi-lo where coordinate d equals g, raycast.cpp:91-100
-template <typename T>
-void at_coord(const T* hi, const T* lo, T g, int d, T* out) {
-    const T dd = hi[d] - lo[d];
-    if (dd == 0.0) { out[0] = hi[0]; out[1] = hi[1]; out[2] = hi[2]; return; }
-    const T wa = (g - lo[d]) / dd, wb = (hi[d] - g) / dd;
-    for (int k = 0; k < 3; k++) out[k] = wa * hi[k] + wb * lo[k];
-}
-
-// does the triangle meet the cube [g0,g1]; raycast.cpp:109-155
-template <typename T>
-bool tri_meets_box(const T (*p)[3], const T* g0, const T* g1) {
-    const T *hi = p[0], *mid = p[1], *lo = p[2];
-    T a[3], b[3];
-    for (int x = 0; x < 3; x++) {
-        // order the three vertex pointers by coordinate x (raycast.cpp:66-85)
-        if (hi[x] < mid[x]) std::swap(hi, mid);
-        if (hi[x] < lo[x]) std::swap(hi, lo);
-        if (mid[x] < lo[x]) std::swap(mid, lo);
-        const int y = (x + 1) % 3, z = (x + 2) % 3;
-        if (g1[x] < lo[x]) return false;
-        at_coord(hi, lo, g1[x], x, a);
-        if (g1[x] < mid[x]) { at_coord(mid, lo, g1[x], x, b); return segment_meets_rect(a, b, g0, g1, y, z); }
-        if (g1[x] <= hi[x]) { at_coord(hi, mid, g1[x], x, b); return segment_meets_rect(a, b, g0, g1, y, z); }
-        if (g0[x] > hi[x]) return false;
-        at_coord(hi, lo, g0[x], x, a);
-        if (g0[x] > mid[x]) { at_coord(hi, mid, g0[x], x, b); return segment_meets_rect(a, b, g0, g1, y, z); }
-        if (g0[x] >= lo[x]) { at_coord(mid, lo, g0[x], x, b); return segment_meets_rect(a, b, g0, g1, y, z); }
-    }
-    return true;
-}
-
-struct Node { int32_t child[8]; int32_t leaf; };
 
 // order-preserving unsigned image of a float / double
 template <typename T> struct OrderedBits;
@@ -106,33 +55,18 @@ template <> struct OrderedBits<double> {
     }
 };
 
-template <typename T>
-struct Part {                      // one independently built subtree
-    std::vector<Node> nodes;
-    std::vector<Box<T>> leaf_box;
-    std::vector<int32_t> leaf_begin;    // into entries (local)
-    std::vector<int32_t> entries;
-    int64_t n_list = 0;
-    T min_edge;
-};
 
 template <typename T>
 struct Builder {
     const Scene<T>& s;
 
-    void child_box(const Box<T>& b, int i, Box<T>& c) const {
-        T mid[3];
-        for (int k = 0; k < 3; k++) mid[k] = (T)(0.5 * (double)b.g0[k] + 0.5 * (double)b.g1[k]);
-        for (int j = 0; j < 3; j++) {
-            c.g0[j] = b.g0[j];
-            c.g1[j] = b.g1[j];
-            if ((i >> j) & 1) c.g0[j] = mid[j]; else c.g1[j] = mid[j];
-        }
-    }
+    void child_box(const Box<T>& b, int i, Box<T>& c) const { geom::child_box(b.g0, b.g1, i, c.g0, c.g1); }
     void filter(const std::vector<int32_t>& in, const Box<T>& c, std::vector<int32_t>& out) const {
         out.clear();
-        for (int32_t t : in)
-            if (tri_meets_box<T>(s.slots[t].p, c.g0, c.g1)) out.push_back(t);
+        for (int32_t t : in) {
+            const auto& p = s.slots[t].p;
+            if (geom::tri_meets_box<T>(p[0], p[1], p[2], c.g0, c.g1)) out.push_back(t);
+        }
     }
     bool is_leaf(size_t n, int level) const { return n <= (size_t)kMaxTriPerNode || level >= kMaxLevel; }
 
@@ -219,7 +153,12 @@ void build_octree(const Scene<T>& s, Octree<T>& o, int threads) {
         for (auto& th : pool) th.join();
         for (int i = 0; i < 8; i++) P.nodes[0].child[i] = merge(P, parts[i]);
     }
+    finish_octree(s, P, o);
+}
 
+template <typename T>
+void finish_octree(const Scene<T>& s, Part<T>& P, Octree<T>& o) {
+    for (int k = 0; k < 3; k++) { o.G0[k] = s.G0[k]; o.G1[k] = s.G1[k]; }
     const int32_t n_leaves = (int32_t)P.leaf_box.size();
     o.min_grid = P.min_edge;
     o.grid_num = (int32_t)((s.G1[0] - s.G0[0]) / o.min_grid);   // raycast.cpp:230
@@ -309,5 +248,7 @@ template bool thresholds_consistent<float>(const Octree<float>&);
 template bool thresholds_consistent<double>(const Octree<double>&);
 template void build_octree<float>(const Scene<float>&, Octree<float>&, int);
 template void build_octree<double>(const Scene<double>&, Octree<double>&, int);
+template void finish_octree<float>(const Scene<float>&, Part<float>&, Octree<float>&);
+template void finish_octree<double>(const Scene<double>&, Part<double>&, Octree<double>&);
 
 }  // namespace radgb

@@ -61,6 +61,7 @@ void usage(const char* argv0, const rad_options& o) {
     fprintf(stderr, "   GPU Options (extensions)\n");
     fprintf(stderr, "       -device <integer>       CUDA device (default 0)\n");
     fprintf(stderr, "       -fp64                   All-FP64 solver (the reference's float->double build)\n");
+    fprintf(stderr, "       -octree_host            Build the octree on the host (default: overlap tests on the GPU)\n");
     fprintf(stderr, "       -autotune               Time both forms of the shooting kernel on the first loops\n");
     fprintf(stderr, "                               and keep the faster (results are the same either way)\n");
     fprintf(stderr, "       -adaptive               Adaptive split variant (config.h = ADAPT + ROLLBACK: serial\n");
@@ -221,6 +222,7 @@ int main(int argc, char* argv[]) {
     int device = 0;
     bool adaptive = false;
     bool autotune = false;
+    bool octree_host = false;
     if (argc < 3) {
         usage(argv[0], o);
         return 1;
@@ -246,7 +248,8 @@ int main(int argc, char* argv[]) {
     }
     static const char* opts[] = {"-debug", "-adapt_area", "-sample_area", "-converge", "-delta_ff",
                                  "-write_cycle", "-zip", "-triangle", "-light", "-o", "-interactive",
-                                 "-jobs", "-parallel_src", "-device", "-fp64", "-adaptive", "-autotune"};
+                                 "-jobs", "-parallel_src", "-device", "-fp64", "-adaptive", "-autotune",
+                                 "-octree_host"};
     const int n_opts = (int)(sizeof opts / sizeof opts[0]);
     const char* in = nullptr;
     const char* out = "./test";
@@ -283,6 +286,7 @@ int main(int argc, char* argv[]) {
             case 14: o.precision = 64; break;
             case 15: adaptive = true; break;
             case 16: autotune = true; break;
+            case 17: octree_host = true; break;
         }
     }
     fprintf(stderr, "[" KGRN "INFO" KWHT "] Input Model " KMAG "%s" KWHT " and Output Prefix " KMAG "%s\n" KWHT,
@@ -299,7 +303,10 @@ int main(int argc, char* argv[]) {
     double t0 = now();
     check(rad_scene_load(in, &o, &scene), "scene input");
     print_log(scene);
-    check(rad_octree_build(scene, o.jobs > 0 ? o.jobs : 0, &tree), "octree");
+    // BuildTree with its overlap tests on the GPU (the same leaves and lists as
+    // the host build, which -octree_host selects)
+    if (octree_host) check(rad_octree_build(scene, o.jobs > 0 ? o.jobs : 0, &tree), "octree");
+    else check(rad_octree_build_device(scene, device, &tree), "octree");
     {
         int64_t nodes = 0, lists = 0;
         rad_octree_info(tree, &nodes, &lists, nullptr, nullptr, nullptr);

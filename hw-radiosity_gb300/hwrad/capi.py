@@ -23,7 +23,7 @@ EXPORTS = [
     "rad_options_default", "rad_last_error", "rad_version",
     "rad_scene_load", "rad_scene_from_arrays", "rad_scene_init", "rad_scene_prepartition",
     "rad_scene_view_get", "rad_scene_write_fin", "rad_scene_log", "rad_scene_free",
-    "rad_octree_build", "rad_octree_info", "rad_octree_cell_coords", "rad_octree_free",
+    "rad_octree_build", "rad_octree_build_device", "rad_octree_tables", "rad_octree_info", "rad_octree_cell_coords", "rad_octree_free",
     "rad_dev_create", "rad_dev_run", "rad_dev_run_timed", "rad_dev_run_profiled", "rad_dev_download", "rad_dev_trace", "rad_dev_stats",
     "rad_dev_set_counting", "rad_dev_set_schedule", "rad_dev_set_layout", "rad_dev_layout", "rad_dev_autotune", "rad_dev_ray_hit", "rad_dev_form_factors", "rad_dev_form_factors_noalloc",
     "rad_dev_destroy",
@@ -95,6 +95,8 @@ def load(path: Optional[str] = None) -> C.CDLL:
         "rad_scene_log": (C.c_char_p, [vp, i32]),
         "rad_scene_free": (None, [vp]),
         "rad_octree_build": (C.c_int, [vp, i32, P(vp)]),
+        "rad_octree_build_device": (C.c_int, [vp, i32, P(vp)]),
+        "rad_octree_tables": (C.c_int, [vp, vp, vp, vp, vp]),
         "rad_octree_info": (C.c_int, [vp, P(i64), P(i64), P(i32), P(i64), P(i32)]),
         "rad_octree_cell_coords": (C.c_int, [vp, i32, vp, i32, vp, vp]),
         "rad_octree_free": (None, [vp]),
@@ -246,9 +248,26 @@ class Scene:
 
 
 class Octree:
-    def __init__(self, scene: Scene, threads: int = 0):
+    def __init__(self, scene: Scene, threads: int = 0, device: Optional[int] = None):
+        """BuildTree on the host (threads), or with the overlap tests on a CUDA
+        device (device=k, rad_octree_build_device)."""
         self.h = C.c_void_p()
-        _check(load().rad_octree_build(scene.h, threads, C.byref(self.h)))
+        self.precision = scene.opts.precision
+        if device is None:
+            _check(load().rad_octree_build(scene.h, threads, C.byref(self.h)))
+        else:
+            _check(load().rad_octree_build_device(scene.h, int(device), C.byref(self.h)))
+
+    def tables(self) -> Dict[str, np.ndarray]:
+        """cell_leaf, leaf_box (n_leaves x 8), leaf_range (n_leaves x 2), entry_tri."""
+        i = self.info()
+        n_cell = int(np.prod(i["dims"]))
+        ft = np.float64 if self.precision == 64 else np.float32
+        out = {"cell_leaf": np.zeros(n_cell, np.int32), "leaf_box": np.zeros((i["leaves"], 8), ft),
+               "leaf_range": np.zeros((i["leaves"], 2), np.int32), "entry_tri": np.zeros(i["entries"], np.int32)}
+        _check(load().rad_octree_tables(self.h, out["cell_leaf"].ctypes.data, out["leaf_box"].ctypes.data,
+                                        out["leaf_range"].ctypes.data, out["entry_tri"].ctypes.data))
+        return out
 
     def info(self) -> Dict[str, object]:
         a, b, e = C.c_int64(), C.c_int64(), C.c_int64()

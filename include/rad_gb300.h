@@ -137,6 +137,18 @@ void rad_scene_free(rad_scene* s);
  * (call before rad_scene_prepartition, as the reference does).  Reports the
  * reference's #TreeNode / #Trilist counts. */
 int rad_octree_build(const rad_scene* s, int32_t threads, rad_octree** out);
+/* The same tree with the triangle-box overlap tests on the device, level by
+ * level (the host files the triangles into the children).  Leaves are
+ * numbered level by level rather than depth first; every leaf's box and list,
+ * the cell-to-leaf map up to that numbering, and the reference's counts are
+ * those of rad_octree_build. */
+int rad_octree_build_device(const rad_scene* s, int32_t device, rad_octree** out);
+/* Copies of the flattened tree (sizes from rad_octree_info): the leaf of each
+ * cell, dims[0]*dims[1]*dims[2]; per leaf its box (g0.xyz, 0, g1.xyz, 0 in
+ * the octree's precision) and [begin, end) range; the triangle of each list
+ * entry.  Any pointer may be null. */
+int rad_octree_tables(const rad_octree* t, int32_t* cell_leaf, void* leaf_box, int32_t* leaf_range,
+                      int32_t* entry_tri);
 int rad_octree_info(const rad_octree* t, int64_t* ref_nodes, int64_t* ref_list, int32_t* n_leaves,
                     int64_t* n_entries, int32_t dims[3]);
 /* Cell coordinates of points q[n] (float or double per the octree's

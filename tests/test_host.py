@@ -177,3 +177,28 @@ def test_fp32_forms_equal_double_expressions(workdir):
     r = subprocess.run([exe, "cpu", "1", "20000000"], capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stdout + r.stderr
     assert r.stdout.split() == ["ok", str(1 << 32), "20000000"]
+
+
+def test_octree_tables(built, workdir):
+    """rad_octree_tables: every cell names a leaf, leaf ranges tile the entry
+    list in order, each list is ascending (the reference's order), and every
+    entry's triangle meets its leaf's box region (bounds overlap)."""
+    s = scenes.room_with_boxes(16, 6, 2, seed=9)
+    tri = s.write(os.path.join(workdir, "tables.tri"))
+    sc = capi.Scene.load(tri, capi.options())
+    t = capi.Octree(sc, 2)
+    i, tb = t.info(), t.tables()
+    assert len(tb["cell_leaf"]) == int(np.prod(i["dims"]))
+    assert tb["cell_leaf"].min() >= 0 and tb["cell_leaf"].max() < i["leaves"]
+    rng = tb["leaf_range"]
+    assert rng[0, 0] == 0 and rng[-1, 1] == i["entries"]
+    assert np.array_equal(rng[1:, 0], rng[:-1, 1])
+    ent = tb["entry_tri"]
+    for b, e in rng:
+        assert np.all(np.diff(ent[b:e]) > 0)
+    assert i["ref_list"] == i["entries"] + i["leaves"]
+    box = tb["leaf_box"]
+    v = sc.view()["p"].reshape(-1, 3, 3)[:sc.view()["n"]]
+    lo, hi = v.min(axis=1), v.max(axis=1)
+    leaf_of_entry = np.repeat(np.arange(len(rng)), rng[:, 1] - rng[:, 0])
+    assert np.all(lo[ent] <= box[leaf_of_entry, 4:7]) and np.all(hi[ent] >= box[leaf_of_entry, 0:3])
