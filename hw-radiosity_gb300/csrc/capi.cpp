@@ -32,6 +32,13 @@ void take_log(rad_scene* h, Scene<T>& s) {
     s.log.clear();
 }
 
+}  // namespace
+
+void take_scene_log(rad_scene* h) {
+    if (h->precision == 32) take_log(h, h->s32); else take_log(h, h->s64);
+}
+
+namespace {
 template <typename T>
 int view_of(const Scene<T>& s, rad_scene_view* v) {
     const size_t n = (size_t)s.trinum;

@@ -20,4 +20,6 @@ struct rad_octree {
 namespace radgb {
 void set_error(const std::string& msg);
 int fail(int code, const std::string& msg);
+// move the scene's info lines into the handle (stdout / stderr streams)
+void take_scene_log(rad_scene* h);
 }  // namespace radgb

@@ -81,7 +81,8 @@ struct Octree {
 template <typename T> int load_tri_text(const char* text, size_t len, const rad_options& o, Scene<T>& s, std::string& err);
 template <typename T> int load_arrays(const float* vtx, const int32_t* frgb, const int32_t* brgb, int32_t n,
                                       const rad_options& o, Scene<T>& s, std::string& err);
-template <typename T> void init_radiosity(Scene<T>& s);              // src/rad.cpp:259-356
+// links = false leaves the neighbour links to the caller (the device form)
+template <typename T> void init_radiosity(Scene<T>& s, bool links = true);   // src/rad.cpp:259-356
 template <typename T> void prepartition(Scene<T>& s);                // src/shade.cpp:556-598
 template <typename T> int write_fin(const Scene<T>& s, const char* prefix, int loop, std::string& err);
 template <typename T> void build_octree(const Scene<T>& s, Octree<T>& o, int threads);  // raycast.cpp:216-233

@@ -62,6 +62,7 @@ void usage(const char* argv0, const rad_options& o) {
     fprintf(stderr, "       -device <integer>       CUDA device (default 0)\n");
     fprintf(stderr, "       -fp64                   All-FP64 solver (the reference's float->double build)\n");
     fprintf(stderr, "       -octree_host            Build the octree on the host (default: overlap tests on the GPU)\n");
+    fprintf(stderr, "       -init_host              Neighbour links on the host (default: on the GPU)\n");
     fprintf(stderr, "       -autotune               Time both forms of the shooting kernel on the first loops\n");
     fprintf(stderr, "                               and keep the faster (results are the same either way)\n");
     fprintf(stderr, "       -adaptive               Adaptive split variant (config.h = ADAPT + ROLLBACK: serial\n");
@@ -223,6 +224,7 @@ int main(int argc, char* argv[]) {
     bool adaptive = false;
     bool autotune = false;
     bool octree_host = false;
+    bool init_host = false;
     if (argc < 3) {
         usage(argv[0], o);
         return 1;
@@ -249,7 +251,7 @@ int main(int argc, char* argv[]) {
     static const char* opts[] = {"-debug", "-adapt_area", "-sample_area", "-converge", "-delta_ff",
                                  "-write_cycle", "-zip", "-triangle", "-light", "-o", "-interactive",
                                  "-jobs", "-parallel_src", "-device", "-fp64", "-adaptive", "-autotune",
-                                 "-octree_host"};
+                                 "-octree_host", "-init_host"};
     const int n_opts = (int)(sizeof opts / sizeof opts[0]);
     const char* in = nullptr;
     const char* out = "./test";
@@ -287,6 +289,7 @@ int main(int argc, char* argv[]) {
             case 15: adaptive = true; break;
             case 16: autotune = true; break;
             case 17: octree_host = true; break;
+            case 18: init_host = true; break;
         }
     }
     fprintf(stderr, "[" KGRN "INFO" KWHT "] Input Model " KMAG "%s" KWHT " and Output Prefix " KMAG "%s\n" KWHT,
@@ -318,7 +321,9 @@ int main(int argc, char* argv[]) {
 
     // DoRadiosity, src/rad.cpp:491-523
     double t2 = now();
-    check(rad_scene_init(scene), "init");
+    // InitRadiosity; the neighbour links on the GPU unless -init_host
+    if (init_host) check(rad_scene_init(scene), "init");
+    else check(rad_scene_init_device(scene, device), "init");
     print_log(scene);
     if (adaptive) return run_adaptive(scene, tree, o, device, out, t2);
     check(rad_scene_prepartition(scene), "pre-partition");

@@ -326,7 +326,7 @@ void link_neighbours(Scene<T>& s) {
 }  // namespace
 
 template <typename T>
-void init_radiosity(Scene<T>& s) {
+void init_radiosity(Scene<T>& s, bool links) {
     T minarea = (T)100000000.0, maxarea = (T)0.0;
     for (int32_t i = 0; i < s.trinum; i++) {
         Slot<T>& tp = s.slots[i];
@@ -344,7 +344,7 @@ void init_radiosity(Scene<T>& s) {
             std::memset(tp.deltaB, 0, sizeof tp.deltaB);
         }
     }
-    link_neighbours(s);
+    if (links) link_neighbours(s);
     s.minarea = minarea;
     s.maxarea = maxarea;
     if (s.opt.sample_area < 0.0f) s.opt.sample_area = (float)((double)maxarea / 100.0);
@@ -624,8 +624,8 @@ template int load_tri_text<float>(const char*, size_t, const rad_options&, Scene
 template int load_tri_text<double>(const char*, size_t, const rad_options&, Scene<double>&, std::string&);
 template int load_arrays<float>(const float*, const int32_t*, const int32_t*, int32_t, const rad_options&, Scene<float>&, std::string&);
 template int load_arrays<double>(const float*, const int32_t*, const int32_t*, int32_t, const rad_options&, Scene<double>&, std::string&);
-template void init_radiosity<float>(Scene<float>&);
-template void init_radiosity<double>(Scene<double>&);
+template void init_radiosity<float>(Scene<float>&, bool);
+template void init_radiosity<double>(Scene<double>&, bool);
 template void prepartition<float>(Scene<float>&);
 template void prepartition<double>(Scene<double>&);
 template int write_fin<float>(const Scene<float>&, const char*, int, std::string&);

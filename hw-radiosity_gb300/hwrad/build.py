@@ -36,7 +36,7 @@ NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "--prec-di
 NVCC_FLAGS += os.environ.get("RAD_NVCC_EXTRA", "").split()
 
 HOST_SRC = ["scene.cpp", "octree.cpp", "capi.cpp"]
-CUDA_SRC = ["rad_dev.cu", "rad_batch.cu", "rad_adapt.cu", "rad_raster.cu", "rad_octree_dev.cu"]
+CUDA_SRC = ["rad_dev.cu", "rad_batch.cu", "rad_adapt.cu", "rad_raster.cu", "rad_octree_dev.cu", "rad_scene_dev.cu"]
 
 
 def _nvcc() -> str:

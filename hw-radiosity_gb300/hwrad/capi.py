@@ -21,7 +21,7 @@ RAD_ERR_ARG, RAD_ERR_IO, RAD_ERR_PARSE, RAD_ERR_CAPACITY, RAD_ERR_CUDA, RAD_ERR_
 
 EXPORTS = [
     "rad_options_default", "rad_last_error", "rad_version",
-    "rad_scene_load", "rad_scene_from_arrays", "rad_scene_init", "rad_scene_prepartition",
+    "rad_scene_load", "rad_scene_from_arrays", "rad_scene_init", "rad_scene_init_device", "rad_scene_prepartition",
     "rad_scene_view_get", "rad_scene_write_fin", "rad_scene_log", "rad_scene_free",
     "rad_octree_build", "rad_octree_build_device", "rad_octree_tables", "rad_octree_info", "rad_octree_cell_coords", "rad_octree_free",
     "rad_dev_create", "rad_dev_run", "rad_dev_run_timed", "rad_dev_run_profiled", "rad_dev_download", "rad_dev_trace", "rad_dev_stats",
@@ -89,6 +89,7 @@ def load(path: Optional[str] = None) -> C.CDLL:
         "rad_scene_load": (C.c_int, [C.c_char_p, P(Options), P(vp)]),
         "rad_scene_from_arrays": (C.c_int, [vp, vp, vp, i32, P(Options), P(vp)]),
         "rad_scene_init": (C.c_int, [vp]),
+        "rad_scene_init_device": (C.c_int, [vp, i32]),
         "rad_scene_prepartition": (C.c_int, [vp]),
         "rad_scene_view_get": (C.c_int, [vp, P(SceneView)]),
         "rad_scene_write_fin": (C.c_int, [vp, C.c_char_p, i32]),
@@ -204,8 +205,13 @@ class Scene:
                                             C.byref(opts), C.byref(h)))
         return cls(h.value, opts)
 
-    def init(self):
-        _check(load().rad_scene_init(self.h))
+    def init(self, device: Optional[int] = None):
+        """InitRadiosity; device=k finds the neighbour links on that GPU
+        (rad_scene_init_device), with the same result."""
+        if device is None:
+            _check(load().rad_scene_init(self.h))
+        else:
+            _check(load().rad_scene_init_device(self.h, int(device)))
 
     def prepartition(self):
         _check(load().rad_scene_prepartition(self.h))

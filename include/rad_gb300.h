@@ -120,6 +120,11 @@ int rad_scene_from_arrays(const float* vtx, const int32_t* frgb, const int32_t* 
  * (exact-coordinate edge matching through a hash instead of the O(N^2) scan,
  * same final links as the sequential scan), SampleArea. */
 int rad_scene_init(rad_scene* s);
+/* The same with the neighbour links found on the device: every candidate
+ * write of the reference's pair scan is made at once, the last one in the
+ * scan's (i, j, v, n) order winning through a 64-bit atomicMax; the links
+ * equal rad_scene_init's.  At most 2^20 triangles. */
+int rad_scene_init_device(rad_scene* s, int32_t device);
 /* PrePartitionTriangles, src/shade.cpp:556-598 (greedy longest-edge
  * bisection of the largest non-light triangles until area < 1 or the pool
  * is full). */

@@ -78,12 +78,13 @@ def test_solver_with_device_octree_matches_fixture(built, workdir, name):
         assert same_bits(v[k], g[k]), k
 
 
-def test_cli_octree_host(built, workdir):
-    """./rad builds the octree on the GPU by default; -octree_host gives the
-    host build, with the same output."""
+@pytest.mark.parametrize("flags", [["-octree_host"], ["-init_host"], ["-octree_host", "-init_host"]])
+def test_cli_host_preparation(built, workdir, flags):
+    """./rad builds the octree and the neighbour links on the GPU by default;
+    -octree_host and -init_host give the host forms, with the same output."""
     tri, argv, idx = write_case("room8", workdir)
-    prefix = os.path.join(workdir, "cli_octhost")
-    r = subprocess.run([build.BIN, tri] + argv + ["-octree_host", "-o", prefix], capture_output=True, text=True,
+    prefix = os.path.join(workdir, "cli_" + "_".join(f.strip("-") for f in flags))
+    r = subprocess.run([build.BIN, tri] + argv + flags + ["-o", prefix], capture_output=True, text=True,
                        timeout=300)
     assert r.returncode == 0, r.stderr
     with open(prefix + ".fin", "rb") as fh:
