@@ -63,3 +63,24 @@ def test_device_entry_points_fail_cleanly_without_device(built, workdir):
     with pytest.raises(capi.RadError) as e:
         capi.Device(sc, tree, o)
     assert e.value.code == capi.RAD_ERR_NODEV
+
+
+def test_device_preparation_fails_cleanly_without_device(built, workdir):
+    """The device forms of the octree build and of InitRadiosity report
+    RAD_ERR_NODEV on a machine without a GPU; the host forms still work."""
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a device is present")
+    from hwrad import scenes
+    s = scenes.room(2, emitter=(0.0, 1.0))
+    tri = s.write(os.path.join(workdir, "nodev2.tri"))
+    o = capi.options_from_argv(s.argv())
+    sc = capi.Scene.load(tri, o)
+    with pytest.raises(capi.RadError) as e:
+        capi.Octree(sc, device=0)
+    assert e.value.code == capi.RAD_ERR_NODEV
+    with pytest.raises(capi.RadError) as e:
+        sc.init(device=0)
+    assert e.value.code == capi.RAD_ERR_NODEV
+    capi.Octree(sc, 1)
+    sc.init()
