@@ -380,7 +380,7 @@ __global__ void k_unshot_total(const double* part, int n, double* out) {
 // The cell table and the list records are expanded on the device from
 // compact host arrays: a leaf index per cell, and per triangle one record
 // group gathered for each list entry naming it.  The records are the ones
-// pack_scene writes (the batched form still packs on the host).
+// pack_scene writes (the batched and adaptive forms still pack on the host).
 template <typename T>
 __global__ void k_expand_cells(const int32_t* __restrict__ cell_leaf, const T* __restrict__ leaf_box,
                                const int32_t* __restrict__ leaf_range, long long n_cell, CellRec<T>* __restrict__ out) {

@@ -17,7 +17,6 @@ namespace dev {
 
 constexpr int kShootThreads = 256;
 constexpr int kSlotsPerWarp = 10;
-constexpr int kSlotsPerCta = kSlotsPerWarp * (kShootThreads / 32);   // 80
 constexpr int kSetupThreads = 1024;
 constexpr int kMaxShooters = 256;
 constexpr double kPiD = 3.1415926535897932;
