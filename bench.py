@@ -19,6 +19,8 @@ scene is smaller than L2.  Also reported:
                 upload of the scene, K steps, download of the results;
   cpu_baseline  the reference's own CPU solver (built from its sources, when
                 available; else the C restatement) on the machine's host cores.
+  hall          the config-3 hall (422,429 slots) in the solver's chosen form
+                and the other one, L2 flushed before each timed step.
 --impl reference times the reference's CPU solver alone on the same workload.
 """
 from __future__ import annotations
@@ -255,6 +257,50 @@ def measure_adaptive(capi, steps, device, with_reference=True):
     return out
 
 
+def measure_hall(capi, device, steps, warmup, flush_l2):
+    """The config-3 hall (40x20x100, 406,684 wall/floor triangles + 300
+    pillars, pre-partitioned to 422,429 slots): shots/s of the single-scene
+    solver in the form it chooses for this scene (form 2: 4 CTAs per SM) and
+    in the other form, L2 flushed before each timed step as in the headline,
+    plus the chosen form's steady state.  The octree and the neighbour links
+    are built on the device."""
+    from hwrad import scenes as S
+    gen = S.hall()
+    tmp = tempfile.mkdtemp(prefix="radhall_")
+    tri = gen.write(os.path.join(tmp, "hall.tri"))
+    o = capi.options_from_argv(gen.argv())
+    t0 = time.time()
+    sc = capi.Scene.load(tri, o)
+    tree = capi.Octree(sc, device=device)
+    sc.init(device=device)
+    sc.prepartition()
+    out = {"workload": "hall 40x20x100, 406,684 triangles + 300 pillars (config 3), FP32",
+           "slots": int(sc.view()["n"]), "host_prep_s": round(time.time() - t0, 2), "steps": steps,
+           "l2": "flushed (512 MB write) before every timed step"}
+    for which in ("chosen", "other"):
+        dv = capi.Device(sc, tree, o, device)
+        if which == "chosen":
+            out["form"] = dv.layout
+        else:
+            dv.set_layout(3 - out["form"])
+            out["other_form"] = dv.layout
+        dv.run(warmup)
+        tot, n_done = 0.0, 0
+        for _ in range(steps):
+            flush_l2()
+            n, conv, ms = dv.run_timed(1)
+            tot += ms
+            n_done += n
+            if conv:
+                break
+        out[f"{which}_flushed_shots_per_s"] = 1000.0 * n_done / tot if tot > 0 else None
+        if which == "chosen":
+            n, _, ms = dv.run_timed(steps * 4)
+            out["chosen_steady_shots_per_s"] = 1000.0 * n / ms if ms > 0 else None
+        dv.close()
+    return out
+
+
 def measure_render(capi, scene, device, reps, with_oracle=True):
     """Headless render of the config-2 result as the viewer shows it (1024x768,
     flat and Gouraud): end-to-end images/s of rad_render_scene and of
@@ -365,6 +411,7 @@ def main():
     ap.add_argument("--batch-iters", type=int, default=100)
     ap.add_argument("--adaptive-steps", type=int, default=100, help="0 skips the adaptive-variant measurement")
     ap.add_argument("--render-reps", type=int, default=5, help="0 skips the headless-render measurement")
+    ap.add_argument("--hall-steps", type=int, default=30, help="0 skips the config-3 hall measurement")
     args = ap.parse_args()
     if os.environ.get("RAD_BENCH_STALL_DUMP"):
         import faulthandler
@@ -493,6 +540,11 @@ def main():
         log("adaptive variant")
         adaptive = measure_adaptive(capi, args.adaptive_steps, local, with_reference=not args.no_cpu_baseline)
 
+    hall = None
+    if args.hall_steps > 0 and rank == 0:
+        log("config-3 hall")
+        hall = measure_hall(capi, local, args.hall_steps, args.warmup, flush_l2)
+
     render = None
     if args.render_reps > 0 and rank == 0:
         log("headless render")
@@ -539,6 +591,7 @@ def main():
         "batched": batched,
         "adaptive": adaptive,
         "render": render,
+        "hall": hall,
         "gpu_launches": done if opts.parallel_src <= 1 else 2 * done,
         "clocks": clocks.summary(),
         "cpu_baseline": cpu,
