@@ -269,14 +269,34 @@ def measure_hall(capi, device, steps, warmup, flush_l2):
     tmp = tempfile.mkdtemp(prefix="radhall_")
     tri = gen.write(os.path.join(tmp, "hall.tri"))
     o = capi.options_from_argv(gen.argv())
+    # first use of the preparation kernels (module load) on a small room
+    wtri = S.room(2).write(os.path.join(tmp, "warm.tri"))
+    ws = capi.Scene.load(wtri, o)
+    capi.Octree(ws, device=device).close()
+    ws.init(device=device)
     t0 = time.time()
     sc = capi.Scene.load(tri, o)
+    t1 = time.perf_counter()
     tree = capi.Octree(sc, device=device)
+    t2 = time.perf_counter()
     sc.init(device=device)
+    t3 = time.perf_counter()
     sc.prepartition()
     out = {"workload": "hall 40x20x100, 406,684 triangles + 300 pillars (config 3), FP32",
            "slots": int(sc.view()["n"]), "host_prep_s": round(time.time() - t0, 2), "steps": steps,
            "l2": "flushed (512 MB write) before every timed step"}
+    # the same preparation in its host forms, for comparison (octree on all
+    # host cores; InitRadiosity's neighbour links by the host hash)
+    sh = capi.Scene.load(tri, o)
+    t4 = time.perf_counter()
+    th = capi.Octree(sh, _nproc())
+    t5 = time.perf_counter()
+    sh.init()
+    t6 = time.perf_counter()
+    out["preparation_ms"] = {"octree_device": round(1e3 * (t2 - t1), 1), "octree_host": round(1e3 * (t5 - t4), 1),
+                             "host_cores": _nproc(), "init_device": round(1e3 * (t3 - t2), 1),
+                             "init_host": round(1e3 * (t6 - t5), 1)}
+    th.close()
     for which in ("chosen", "other"):
         dv = capi.Device(sc, tree, o, device)
         if which == "chosen":
