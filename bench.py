@@ -39,6 +39,36 @@ REPO = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(REPO, "hw-radiosity_gb300"))
 
 WORKLOAD = "room64x64_boxes16 (61,440 triangles, config 2), FP32, plain single-scene form"
+L2_NOTE = "GPU arm: flushed (512 MB write) before every timed step; CPU arm: not applicable"
+# the k_shoot sources whose ncu capture gave the committed DRAM traffic figure
+KERNEL_SOURCES = ("hw-radiosity_gb300/csrc/rad_dev.cu", "hw-radiosity_gb300/csrc/rad_kernels.cuh")
+TRAFFIC_FILE = "profiles/k_shoot_room64_boxes16.traffic.txt"
+
+
+def kernel_source_sha():
+    import hashlib
+    h = hashlib.sha256()
+    for f in KERNEL_SOURCES:
+        with open(os.path.join(REPO, f), "rb") as fh:
+            h.update(fh.read())
+    return h.hexdigest()[:16]
+
+
+def committed_traffic():
+    """DRAM bytes per k_shoot launch from the committed ncu capture, and whether
+    it was captured from the kernel sources as they are now."""
+    path = os.path.join(REPO, TRAFFIC_FILE)
+    if not os.path.exists(path):
+        return None, None
+    vals = {}
+    for line in open(path):
+        if ":" in line and not line.startswith("#"):
+            k, v = line.split(":", 1)
+            vals[k.strip()] = v.strip()
+    traffic = int(vals["dram_bytes_per_launch"]) if "dram_bytes_per_launch" in vals else None
+    src = vals.get("kernel_sources_sha256_16")
+    return traffic, {"captured_from_sources": src, "current_sources": kernel_source_sha(),
+                     "matches": src == kernel_source_sha()}
 BYTES_PER_SLOT = 176       # selection key 16 + receiver read 112 + receiver write 48
 BYTES_PER_CELL = 8
 BYTES_PER_TRI_TEST = 24
@@ -134,87 +164,201 @@ def _scene_file(tmp):
     return sc, sc.write(os.path.join(tmp, "config2.tri"))
 
 
-def cpu_reference(tri, argv, warmup, steps, prefer_ref=True, jobs=None):
-    """Time the reference's CPU solver (or the C restatement) over steps
-    [warmup, warmup+steps) from its per-step timestamps."""
+def cpu_reference(tri, argv, warmup, steps, jobs=None):
+    """Time the reference's CPU solver, built from its sources with its own
+    Makefile flags (oracle/_ref/rad_ref_shipped), over steps [warmup,
+    warmup+steps) from its per-step timestamps.  There is no fallback: without
+    the reference build this raises."""
     sys.path.insert(0, os.path.join(REPO, "oracle"))
     import runner
     cores = _nproc()
-    if prefer_ref and not os.path.exists(runner.REF32):
-        try:
-            runner.build_ref()
-        except Exception:
-            pass
-    if prefer_ref and os.path.exists(runner.REF32):
-        binary, kind, jobs = runner.REF32, "reference", (jobs or cores)
-    else:
-        runner.build_oracle()
-        binary, kind, jobs = runner.ORACLE32, "port", 1
+    if not os.path.exists(runner.REF_SHIPPED):
+        runner.build_ref()
+    if not os.path.exists(runner.REF_SHIPPED):
+        raise RuntimeError("the reference CPU solver (oracle/_ref/rad_ref_shipped) is not built: "
+                           "no reference sources were staged under oracle/_ref")
+    jobs = jobs or cores
     wd = tempfile.mkdtemp(prefix="radcpu_")
     times = os.path.join(wd, "times.txt")
     t0 = time.time()
-    runner.run(binary, tri, list(argv) + ["-jobs", str(jobs)], steps=warmup + steps,
-               env={"RAD_TIMES": times}, workdir=wd, timeout=3600)
+    out = runner.run(runner.REF_SHIPPED, tri, list(argv) + ["-jobs", str(jobs)], steps=warmup + steps,
+                     env={"RAD_TIMES": times}, workdir=wd, timeout=3600)
     wall = time.time() - t0
     stamps = [float(x) for x in open(times).read().split()]
     # stamp k = start of step k (0-based); the last stamp is the call that stopped the loop
     a, b = stamps[warmup], stamps[min(warmup + steps, len(stamps) - 1)]
     n = min(warmup + steps, len(stamps) - 1) - warmup
-    return {"value": n / (b - a) if b > a else None, "unit": "shots/s", "cores": jobs, "kind": kind,
+    return {"value": n / (b - a) if b > a else None, "unit": "shots/s", "cores": jobs, "kind": "reference",
+            "build": runner.REF_SHIPPED_FLAGS,
             "sample": f"steps {warmup}..{warmup + n} of the workload ({n} shooter steps after {warmup} "
                       f"warm-up steps; {wall:.1f} s wall including the solver's own init)",
-            "seconds": b - a}
+            "seconds": b - a, "slots": int(out["dump"]["n"])}
 
 
-def measure_batched(capi, n_scenes, warmup, iters, device):
-    """Config 4: n_scenes seeded rooms (triangles log-uniform in [500, 50000],
-    0-32 boxes), each converging at 1e-4 of its emitter key.  Batched: every
-    running scene does one shooter step per iteration, all in one launch.
-    Plain: the single-scene solver on each scene in turn, over the same
-    iterations.  Device time from CUDA events on each solver's stream."""
-    from hwrad import scenes as S
-    t0 = time.time()
-    gens = S.batch_rooms(n_scenes, seed=4000)
-    preps = []
-    for g in gens:
+SIZE_BANDS = ((0, 2000, "<2k"), (2000, 10000, "2k-10k"), (10000, 1 << 40, ">10k"))
+
+
+def prepare_scenes(capi, gens, device, threads=None):
+    """Scenes from the generator's arrays; octree and InitRadiosity's
+    neighbour links on the device, pre-partition on the host.  Scenes are
+    prepared on several host threads at once (each with its own stream and
+    device scratch in the library); the calls release the GIL."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    def one(g):
         o = capi.options_from_argv(g.argv())
         sc = capi.Scene.from_arrays(g.vtx, g.frgb, g.brgb, o)
-        tr = capi.Octree(sc, _nproc())
-        sc.init()
+        tr = capi.Octree(sc, device=device)
+        sc.init(device=device)
         sc.prepartition()
-        preps.append((sc, tr, o))
-    prep_s = time.time() - t0
-    log(f"batch: {n_scenes} scenes prepared in {prep_s:.1f} s")
-    tris = [p[0].view()["n"] for p in preps]
+        return sc, tr, o
+    with ThreadPoolExecutor(max_workers=threads or min(16, _nproc())) as ex:
+        return list(ex.map(one, gens))
+
+
+def _batch(capi, preps, device, form=None):
     b = capi.Batch([p[0] for p in preps], [p[1] for p in preps], [p[2] for p in preps], device)
+    if form:
+        b.set_form(form)
+    return b
+
+
+def measure_batched(capi, n_scenes, warmup, iters, device, world=1, rank=0, ranks=None):
+    """Config 4: n_scenes seeded rooms (triangles log-uniform in [500, 50000],
+    0-32 boxes), each converging at 1e-4 of its emitter key.  Batched: every
+    running scene does one shooter step per iteration, all in one launch, in
+    the kernel form the autotuner picks.  Plain: the single-scene solver on
+    each scene in turn, over the same steps.  Device time from CUDA events on
+    each solver's stream.  Each scene's batched trace and accB/deltaB are
+    compared with its plain run bit for bit; no ratio is given if any differs.
+    With several ranks, each takes a share of the scenes balanced by triangle
+    count (no exchange of data) and the totals are summed over ranks."""
+    import numpy as np
+    from hwrad import scenes as S, shard
+    gens_all = S.batch_rooms(n_scenes, seed=4000)
+    share = shard.partition_scenes([len(g.vtx) for g in gens_all], world)[rank]
+    gens = [gens_all[i] for i in share]
+    # first use of the preparation kernels (module load) on a small room
+    prepare_scenes(capi, [S.room(2)], device)
+    t0 = time.perf_counter()
+    preps = prepare_scenes(capi, gens, device)
+    prep_s = time.perf_counter() - t0
+    log(f"batch: {len(gens)} scenes prepared (device octree and links) in {prep_s:.2f} s")
+    tris = [p[0].view()["n"] for p in preps]
+    t0 = time.perf_counter()
+    b = _batch(capi, preps, device)
+    create_s = time.perf_counter() - t0
+    form = b.autotune(4, 2)
     b.run(warmup)
-    s0 = sum(b.scene_stats(i)[0] for i in range(n_scenes))
+    s0 = [b.scene_stats(i)[0] for i in range(len(preps))]
+    K = max(s0)                      # iterations before the timed window
     it, active, ms = b.run_timed(iters)
-    s1 = sum(b.scene_stats(i)[0] for i in range(n_scenes))
-    st = b.stats()
-    dev_bytes = st["device_bytes"]
-    b.close()
-    batched = (s1 - s0) / (ms / 1000.0) if ms > 0 else None
-    log(f"batch: {it} iterations, {s1 - s0} shots in {ms:.1f} ms")
+    s1 = [b.scene_stats(i)[0] for i in range(len(preps))]
+    shots = sum(s1) - sum(s0)
+    dev_bytes = b.stats()["device_bytes"]
+    log(f"batch: form {form}, {it} iterations, {shots} shots in {ms:.1f} ms")
+    # exact walk counts over the same iterations (counting pass on a fresh batch)
+    bc = _batch(capi, preps, device, form)
+    bc.run(K)
+    bc.set_counting(True)
+    c0 = bc.stats()
+    bc.run(iters)
+    c1 = bc.stats()
+    bc.close()
+    cnt = {k: c1[k] - c0[k] for k in ("rays", "cells", "tri_tests", "se_tests")}
+    slot_steps = sum(n * (s1[i] - s0[i]) for i, n in enumerate(tris))
+    alg = slot_steps * BYTES_PER_SLOT + cnt["cells"] * BYTES_PER_CELL + cnt["tri_tests"] * BYTES_PER_TRI_TEST + \
+        cnt["se_tests"] * BYTES_PER_SE_TEST
+    # the same window per scene-size band, each band batched on its own
+    bands = {}
+    for lo, hi, name in SIZE_BANDS:
+        idx = [i for i, n in enumerate(tris) if lo <= n < hi]
+        if not idx:
+            continue
+        bb = _batch(capi, [preps[i] for i in idx], device, form)
+        bb.run(K)
+        s0b = sum(bb.scene_stats(j)[0] for j in range(len(idx)))
+        _, _, msb = bb.run_timed(iters)
+        s1b = sum(bb.scene_stats(j)[0] for j in range(len(idx)))
+        bb.close()
+        bands[name] = {"scenes": len(idx), "triangles": int(sum(tris[i] for i in idx)), "shots": s1b - s0b,
+                       "batched_ms": msb, "idx": idx}
+    # plain: the single-scene solver scene by scene over the same steps, and parity
     plain_ms = 0.0
     plain_shots = 0
+    per_plain = []
+    bad = []
     for k, (sc, tr, o) in enumerate(preps):
-        if k % 32 == 0:
-            log(f"plain: scene {k}")
         d = capi.Device(sc, tr, o, device)
-        d.run(warmup)
+        if s0[k]:
+            d.run(s0[k])
         n, conv, m = d.run_timed(iters)
         plain_ms += m
         plain_shots += n
+        per_plain.append((n, m))
+        same = n == s1[k] - s0[k] and np.array_equal(d.trace(), b.trace(k))
+        d.download(sc)
+        v = sc.view()
+        acc, db = v["accB"].copy(), v["deltaB"].copy()
         d.close()
-    plain = plain_shots / (plain_ms / 1000.0) if plain_ms > 0 else None
-    log(f"plain: {plain_shots} shots in {plain_ms:.1f} ms")
-    return {"workload": f"{n_scenes} rooms (config 4), {sum(tris):,} triangles, {min(tris)}-{max(tris)} per scene",
-            "iterations": it, "shots": s1 - s0, "active_scenes_end": active,
+        b.download(k, sc)
+        v = sc.view()
+        same = same and np.array_equal(acc.view(np.uint32), v["accB"].view(np.uint32)) and \
+            np.array_equal(db.view(np.uint32), v["deltaB"].view(np.uint32))
+        if not same:
+            bad.append(share[k])
+    b.close()
+    log(f"plain: {plain_shots} shots in {plain_ms:.1f} ms; scenes differing: {bad}")
+    for name, v in bands.items():
+        ps = sum(per_plain[i][0] for i in v["idx"])
+        pm = sum(per_plain[i][1] for i in v["idx"])
+        bs = v["shots"] / (v["batched_ms"] / 1000.0) if v["batched_ms"] > 0 else None
+        pl = ps / (pm / 1000.0) if pm > 0 else None
+        v.update({"batched_shots_per_s": bs, "plain_shots_per_s": pl,
+                  "batched_over_plain": bs / pl if bs and pl and not bad else None})
+        del v["idx"]
+    # end to end through the C ABI: fresh scenes from the generator's arrays,
+    # device preparation, upload, the same iterations, download of every scene
+    t0 = time.perf_counter()
+    ep = prepare_scenes(capi, gens, device)
+    be = _batch(capi, ep, device, form)
+    be.run(K + iters)
+    e_shots = sum(be.scene_stats(i)[0] for i in range(len(ep)))
+    for i, (sc, _, _) in enumerate(ep):
+        be.download(i, sc)
+    e2e_s = time.perf_counter() - t0
+    est = be.stats()
+    be.close()
+    # totals over ranks (scenes are sharded; each rank reports its share)
+    red_sum = ranks.sum if ranks else (lambda x: x)
+    red_max = ranks.max if ranks else (lambda x: x)
+    shots_t, plain_shots_t = red_sum(shots), red_sum(plain_shots)
+    ms_t, plain_ms_t, e2e_t = red_max(ms), red_sum(plain_ms), red_max(e2e_s)
+    n_bad = int(red_sum(len(bad)))
+    batched = shots_t / (ms_t / 1000.0) if ms_t > 0 else None
+    plain = plain_shots_t / (plain_ms_t / 1000.0) if plain_ms_t > 0 else None
+    achieved = alg / (ms / 1000.0) / 1e9 if ms > 0 else None
+    peak, peak_kind = _peaks()
+    all_tris = [len(g.vtx) for g in gens_all]
+    return {"workload": f"{n_scenes} rooms (config 4), {sum(all_tris):,} input triangles, "
+                        f"{min(all_tris)}-{max(all_tris)} per scene",
+            "ranks": world, "scenes_this_rank": len(gens), "slots_this_rank": int(sum(tris)),
+            "form": form, "iterations": it, "shots": shots_t, "active_scenes_end": active,
+            "parity": "bit-identical" if n_bad == 0 else f"DIFFERS in {n_bad} scenes (first: {bad[:8]})",
             "batched_shots_per_s": batched, "plain_shots_per_s": plain,
-            "batched_over_plain": batched / plain if batched and plain else None,
-            "batched_ms_per_iter": ms / max(it, 1), "plain_shots": plain_shots,
-            "device_bytes": dev_bytes, "host_prep_s": round(prep_s, 1),
+            "batched_over_plain": batched / plain if batched and plain and n_bad == 0 else None,
+            "rays_per_s": cnt["rays"] / (ms / 1000.0) if ms > 0 else None,
+            "batched_ms_per_iter": ms / max(it, 1), "plain_shots": plain_shots_t,
+            "bands": bands,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak if achieved else None, "kernel": "k_batch_shoot",
+                         "peak_kind": f"{peak_kind} hbm_gbs", "alg_bytes_per_iter": alg / max(it, 1),
+                         "counts_per_iter": {k: v / max(it, 1) for k, v in cnt.items()}},
+            "e2e": {"value": e_shots * world / e2e_t if e2e_t > 0 else None, "unit": "shots/s",
+                    "seconds": e2e_t, "h2d_bytes": est["h2d_bytes"],
+                    "note": "generator arrays -> device octree + links, host pre-partition, rad_batch_create "
+                            "(upload), warm-up and timed iterations, download of every scene"},
+            "device_bytes": dev_bytes, "prep_s": round(prep_s, 3), "create_s": round(create_s, 3),
             "l2": "batch inputs exceed L2; plain timed without flush (graph chunks)"}
 
 
@@ -240,7 +384,8 @@ def measure_adaptive(capi, steps, device, with_reference=True):
     out = {"workload": "room 100^3, 4 boxes, 960 triangles splitting toward the 40,000 cap, -converge 5",
            "steps": n, "slots_end": st["n_slots"], "steps_per_s": n / dt if dt > 0 else None,
            "rays": st["rays"], "splits": st["splits"], "host_form_factors": st["host_points"],
-           "sample_points": st["samples"]}
+           "sample_points": st["samples"], "device_sample_points": st["device_points"],
+           "speculations": st["speculations"], "split_candidates": st["split_candidates"]}
     ad.close()
     if with_reference:
         sys.path.insert(0, os.path.join(REPO, "oracle"))
@@ -274,6 +419,7 @@ def measure_hall(capi, device, steps, warmup, flush_l2):
     ws = capi.Scene.load(wtri, o)
     capi.Octree(ws, device=device).close()
     ws.init(device=device)
+    ws.close()
     t0 = time.time()
     sc = capi.Scene.load(tri, o)
     t1 = time.perf_counter()
@@ -297,6 +443,7 @@ def measure_hall(capi, device, steps, warmup, flush_l2):
                              "host_cores": _nproc(), "init_device": round(1e3 * (t3 - t2), 1),
                              "init_host": round(1e3 * (t6 - t5), 1)}
     th.close()
+    sh.close()
     for which in ("chosen", "other"):
         dv = capi.Device(sc, tree, o, device)
         if which == "chosen":
@@ -384,12 +531,18 @@ class Ranks:
             self.dist.barrier()
         self.sync()
 
-    def max(self, x):
+    def _reduce(self, x, op):
         if not self.dist:
             return x
         t = self.torch.tensor([x], dtype=self.torch.float64, device="cuda" if self.cuda else "cpu")
-        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        self.dist.all_reduce(t, op=op)
         return float(t.item())
+
+    def max(self, x):
+        return self._reduce(x, self.dist.ReduceOp.MAX if self.dist else None)
+
+    def sum(self, x):
+        return self._reduce(x, self.dist.ReduceOp.SUM if self.dist else None)
 
     def close(self):
         if self.dist:
@@ -401,20 +554,29 @@ def replica_value(world, steps_per_rank, worst_ms):
     return world * steps_per_rank / (worst_ms / 1000.0) if worst_ms > 0 else None
 
 
+def bench_config(slots, world):
+    """The workload keys both arms report (the reference arm and ours)."""
+    return {"workload": WORKLOAD, "slots": int(slots), "l2": L2_NOTE, "parallelism": f"replicas x{world}"}
+
+
 def run_reference_arm(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
     with tempfile.TemporaryDirectory() as tmp:
         sc, tri = _scene_file(tmp)
-        res = cpu_reference(tri, sc.argv(), args.warmup, args.steps)
+        try:
+            res = cpu_reference(tri, sc.argv(), args.warmup, args.steps)
+        except Exception as exc:
+            print(json.dumps({"impl": "reference", "unavailable": f"{exc}".splitlines()[0]}))
+            return 0
     line = {"metric": "shots/s", "value": res["value"], "unit": "shots/s", "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1000.0 / res["value"] if res["value"] else None,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded generator, hwrad.scenes.config2)", "impl": "reference",
-            "config": {"workload": WORKLOAD, "l2": "n/a (CPU)"},
+            "config": bench_config(res["slots"], args.gpus),
             "cpu_baseline": {"value": res["value"], "unit": "shots/s", "cores": res["cores"], "kind": res["kind"],
-                             "sample": res["sample"]},
+                             "build": res["build"], "sample": res["sample"]},
             "e2e": {"value": res["value"], "unit": "shots/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
     return 0
@@ -433,9 +595,6 @@ def main():
     ap.add_argument("--render-reps", type=int, default=5, help="0 skips the headless-render measurement")
     ap.add_argument("--hall-steps", type=int, default=30, help="0 skips the config-3 hall measurement")
     args = ap.parse_args()
-    if os.environ.get("RAD_BENCH_STALL_DUMP"):
-        import faulthandler
-        faulthandler.dump_traceback_later(float(os.environ["RAD_BENCH_STALL_DUMP"]), repeat=True, file=sys.stderr)
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
@@ -526,7 +685,7 @@ def main():
     torch.cuda.synchronize()
     te1 = time.perf_counter()
     e2e_s = max_over_ranks(te1 - te0)
-    dev_bytes = dev2.stats()["device_bytes"]
+    h2d_bytes = dev2.stats()["h2d_bytes"]
     dev2.close()
     clocks.stop()
 
@@ -537,23 +696,18 @@ def main():
     avg_shoot_s = shoot_ms / 1000.0 / max(done, 1)
     peak, peak_kind = _peaks()
     achieved = per_launch / avg_shoot_s / 1e9 if avg_shoot_s > 0 else None
-    traffic = None
-    tp = os.path.join(REPO, "profiles", "k_shoot_room64_boxes16.traffic.txt")
-    if os.path.exists(tp):
-        for line in open(tp):
-            if line.startswith("dram_bytes_per_launch:"):
-                traffic = int(line.split(":")[1])
+    traffic, traffic_src = committed_traffic()
 
     value = replica_value(world, done, worst_ms)
-    h2d = 0
-    # the upload: slot records (6 x 16 B per slot, 3 of them x3) + octree; approximated by device bytes held
-    h2d = dev_bytes / max(args.warmup + done, 1)
+    # bytes rad_dev_create copied to the device (counted by the library), and
+    # the download of accB + deltaB (4 records of 16 B per slot), per step
+    h2d = h2d_bytes / max(args.warmup + done, 1)
     d2h = n_slots * 16 * 4 / max(args.warmup + done, 1)
 
     log(f"e2e {e2e_s:.3f} s")
     batched = None
     if args.batch_scenes > 0:
-        batched = measure_batched(capi, args.batch_scenes, args.warmup, args.batch_iters, local)
+        batched = measure_batched(capi, args.batch_scenes, args.warmup, args.batch_iters, local, world, rank, ranks)
 
     adaptive = None
     if args.adaptive_steps > 0:
@@ -578,8 +732,8 @@ def main():
         except Exception as exc:
             cpu = {"value": None, "unit": "shots/s", "cores": _nproc(), "kind": "reference",
                    "sample": f"failed: {exc}"}
-        cpu = {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")}
-        if cpu["kind"] == "reference" and cpu["cores"] > 1:
+        cpu = {k: cpu.get(k) for k in ("value", "unit", "cores", "kind", "build", "sample")}
+        if cpu["value"] is not None and cpu["cores"] > 1:
             try:
                 one = cpu_reference(tri, argv, 2, 12, jobs=1)
                 cpu["one_thread"] = {k: one[k] for k in ("value", "cores", "sample")}
@@ -591,8 +745,8 @@ def main():
         "warmup": args.warmup, "ms_per_step": worst_ms / max(done, 1), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded generator, hwrad.scenes.config2)",
-        "config": {"workload": WORKLOAD, "slots": n_slots, "l2": "flushed (512 MB write) before every timed step",
-                   "parallelism": f"replicas x{world}", "host_prep_s": round(host_prep_s, 3)},
+        "config": bench_config(n_slots, world),
+        "host_prep_s": round(host_prep_s, 3),
         "rays_per_s": d["rays"] / (worst_ms / 1000.0) if worst_ms > 0 else None,
         "rays_per_step": d["rays"] / max(done, 1),
         "unshot_power": {"after_warmup": unshot_start, "after_timed_steps": unshot_end,
@@ -602,6 +756,7 @@ def main():
         "kernels_ms_per_step": {"k_setup": setup_ms / max(done, 1), "k_shoot": shoot_ms / max(done, 1)},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak if achieved else None, "traffic": traffic,
+                     "traffic_capture": traffic_src,
                      "kernel": "k_shoot", "peak_kind": f"{peak_kind} hbm_gbs (burst)",
                      "alg_bytes_per_launch": per_launch,
                      "counts_per_launch": {k: v / max(done, 1) for k, v in d.items()}},

@@ -8,15 +8,27 @@
 // current slot (visited again), or rewrites an earlier neighbour, and the
 // sample points come from one global rand() stream.  But almost all the rays
 // are independent: the three corner form factors and the centre form factor
-// of every receiver against the step's shooter.  So each step
+// of every receiver against the step's shooter, and the form factors of the
+// rand() sample points a receiver draws when those agree.  So each step
 //   1. the device computes those four form factors for every slot
-//      (k_adapt_ff, one thread per slot and point);
+//      (k_adapt_ff, one thread per slot and point), runs the delta-FF test of
+//      every receiver (k_adapt_test), numbers the sample points of the
+//      receivers that pass it by a scan of their counts (the stream
+//      compaction of the sampling receivers), and evaluates every one of them
+//      at the rand() triple it gets if no receiver breaks its sample loop early
+//      (k_adapt_samples, reading a device ring of the host's rand() stream);
 //   2. the host runs the reference's receiver loop in order, taking a
 //      precomputed value whenever its inputs are unchanged -- the receiver was
-//      not written by a split earlier in this step and the shooter slot was
-//      not either -- and otherwise evaluating the same walk and form-factor
-//      code on the host (it is compiled for both), as for sample points and
-//      re-shaded neighbours.
+//      not written by a split earlier in this step, the shooter slot was not
+//      either, and (for sample points) the stream is at the triple the value
+//      was drawn from.  When a sample loop broke early or a rewritten receiver
+//      drew points, the next receiver that samples starts a new speculation
+//      from the stream's position (another k_adapt_samples launch).  Values
+//      whose inputs changed -- rewritten or appended receivers, re-shaded
+//      neighbours -- are evaluated on the host with the same walk and
+//      form-factor code (it is compiled for both).
+// The splits themselves (bisection, neighbour links, rollback) stay on the
+// host: each one changes what the rest of the step sees.
 // The result is bit-identical to the reference's adaptive build: every value
 // is computed by the same arithmetic from the same inputs.
 #include <cuda_runtime.h>
@@ -61,6 +73,141 @@ __global__ void k_adapt_ff(Slots<T> S, Grid<T> G, const Shooter<T>* __restrict__
         if (r) atomicAdd(&st->rays, (unsigned long long)r);
         if (cap) atomicAdd(&st->capped, (unsigned long long)cap);
         if (lp) atomicAdd(&st->loops, (unsigned long long)lp);
+    }
+}
+
+// ------------------------------------------------------------------ sample points
+// Shade's delta-FF test (shade.cpp:481-508) of every receiver against the
+// step's shooter, from its corner and centre form factors: a receiver whose
+// corner mean and centre agree draws n = (int)(area / sample_area) rand()
+// sample points, unless it is small (area < adapt_area), the pool is full or
+// its area is below 1e-8.  ntask[s] = n for those receivers (0 for the others,
+// for receivers the host does not visit -- the shooter, dead slots, closed
+// ones -- and above kMaxSpecSamples); *n_split counts the receivers whose
+// test fails (split candidates).  The exclusive scan of ntask numbers every
+// sample point of the step (the stream compaction of the sampling receivers):
+// with no split or early break, sample point t of the step is drawn from rand()
+// triple base + t.
+constexpr int kMaxSpecSamples = 1 << 14;
+
+template <typename T>
+__global__ void k_adapt_test(Slots<T> S, int n, const T* __restrict__ ff, const uint8_t* __restrict__ open,
+                             float adapt_area, float delta_ff, float sample_area, int pool_full, long long* ntask,
+                             unsigned* n_split) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    long long k = 0;
+    if (open[s]) {
+        const T area = S.ctr[s].w;
+        if (!(area < adapt_area) && !pool_full && !((double)area < 1e-8)) {
+            const T f0 = ff[4 * s], f1 = ff[4 * s + 1], f2 = ff[4 * s + 2], fc = ff[4 * s + 3];
+            const T ground = (T)((double)(f0 + f1 + f2) / 3.0);
+            const T dff = (T)fabs((double)(ground - fc));
+            if (dff < delta_ff) {
+                const T q = area / sample_area;
+                if (q >= (T)1 && q < (T)(kMaxSpecSamples + 1)) k = (int)q;
+            } else {
+                atomicAdd(n_split, 1u);
+            }
+        }
+    }
+    ntask[s] = k;
+}
+
+// exclusive scan of v[0..n) into out[0..n], out[n] = total: tiles of 1024
+// scanned per CTA, the tile sums by one CTA, then the tile offsets added
+constexpr int kScanTile = 1024;
+
+__device__ __forceinline__ long long block_excl_scan(long long x, long long* total) {
+    __shared__ long long ws[32];
+    __shared__ long long wtot;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    long long inc = x;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const long long y = __shfl_up_sync(kFull, inc, d);
+        if (lane >= d) inc += y;
+    }
+    if (lane == 31) ws[wid] = inc;
+    __syncthreads();
+    if (wid == 0) {
+        const int nw = blockDim.x >> 5;
+        long long w = lane < nw ? ws[lane] : 0, wi = w;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const long long y = __shfl_up_sync(kFull, wi, d);
+            if (lane >= d) wi += y;
+        }
+        if (lane < nw) ws[lane] = wi - w;
+        if (lane == nw - 1) wtot = wi;
+    }
+    __syncthreads();
+    const long long r = ws[wid] + inc - x;
+    *total = wtot;
+    __syncthreads();
+    return r;
+}
+
+__global__ void __launch_bounds__(kScanTile) k_scan_tiles(const long long* v, int n, long long* out, long long* tile_sum) {
+    const int i = blockIdx.x * kScanTile + threadIdx.x;
+    long long tot;
+    const long long e = block_excl_scan(i < n ? v[i] : 0, &tot);
+    if (i < n) out[i] = e;
+    if (threadIdx.x == 0) tile_sum[blockIdx.x] = tot;
+}
+
+__global__ void __launch_bounds__(kScanTile) k_scan_sums(long long* tile_sum, int tiles, long long* out, int n) {
+    long long carry = 0;
+    for (int b = 0; b < tiles; b += kScanTile) {
+        const int i = b + threadIdx.x;
+        long long tot;
+        const long long e = block_excl_scan(i < tiles ? tile_sum[i] : 0, &tot);
+        if (i < tiles) tile_sum[i] = carry + e;
+        carry += tot;
+    }
+    if (threadIdx.x == 0) out[n] = carry;
+}
+
+__global__ void __launch_bounds__(kScanTile) k_scan_add(const long long* tile_off, int n, long long* out) {
+    const int i = blockIdx.x * kScanTile + threadIdx.x;
+    if (i < n) out[i] += tile_off[blockIdx.x];
+}
+
+// Sample points [start, end) of the step (end clipped to the step's total),
+// point t drawn from rand() triple base + (t - start) of the ring: the
+// receiver (largest s with toff[s] <= t), GetPointInTriangle (shade.cpp:49-68)
+// and the point's AdaptCalFF(CalFF(...)) (shade.cpp:499-502).  Written to host
+// memory: ff[t] and the walk counters of its rays (rays | capped << 8 |
+// loops << 16), added on the host only for points it uses.
+template <typename T>
+__global__ void k_adapt_samples(Slots<T> S, Grid<T> G, const Shooter<T>* __restrict__ shp,
+                                const long long* __restrict__ toff, int n, long long start, long long end,
+                                long long base, const int32_t* __restrict__ ring, long long ring_len,
+                                T* __restrict__ out_ff, int* __restrict__ out_code) {
+    const long long total = toff[n];
+    if (end > total) end = total;
+    const Shooter<T> sh = *shp;
+    for (long long t = start + blockIdx.x * (long long)blockDim.x + threadIdx.x; t < end;
+         t += (long long)gridDim.x * blockDim.x) {
+        int lo = 0, hi = n - 1;        // toff is non-decreasing; toff[0] = 0 <= t
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (toff[mid] <= t) lo = mid; else hi = mid - 1;
+        }
+        const int s = lo;
+        const long long tri = base + (t - start);
+        T r1 = (T)ring[(3 * tri) % ring_len], r2 = (T)ring[(3 * tri + 1) % ring_len],
+          r3 = (T)ring[(3 * tri + 2) % ring_len];
+        const T tot = r1 + r2 + r3;
+        r1 /= tot; r2 /= tot; r3 /= tot;
+        const Q4<T> p0 = S.vtx[s * 3], p1 = S.vtx[s * 3 + 1], p2 = S.vtx[s * 3 + 2];
+        const T pt[3] = {r1 * p0.x + r2 * p1.x + r3 * p2.x, r1 * p0.y + r2 * p1.y + r3 * p2.y,
+                         r1 * p0.z + r2 * p1.z + r3 * p2.z};
+        const Q4<T> nn = S.nrm[s];
+        const T nd[3] = {nn.x, nn.y, nn.z};
+        Cnt c = {0, 0, 0, 0, 0, 0, 0, 0};
+        out_ff[t] = corner_ff<T, false>(sh, pt, nd, nn.w, (int)S.frgb[s].w, G, c);
+        out_code[t] = (int)(c.rays | (c.capped << 8) | (c.loops << 16));
     }
 }
 
@@ -123,6 +270,29 @@ public:
     }
 };
 
+// The rand() stream with absolute positions: values are generated ahead on
+// demand and kept until consumed, so the device can be given future draws.
+class RandStream {
+    LibcRand g_;
+    std::vector<int32_t> buf_;
+    long long base_ = 0;   // absolute index of buf_[0]
+
+public:
+    long long pos = 0;     // draws consumed so far
+    int32_t at(long long i) {
+        while (base_ + (long long)buf_.size() <= i) buf_.push_back(g_.next());
+        return buf_[(size_t)(i - base_)];
+    }
+    int next() {
+        const int32_t v = at(pos++);
+        if (pos - base_ > (1 << 20)) {
+            buf_.erase(buf_.begin(), buf_.begin() + (size_t)(pos - base_));
+            base_ = pos;
+        }
+        return v;
+    }
+};
+
 template <typename T>
 inline T slot_nlen(const Slot<T>& t) { return (T)std::sqrt(t.n[0] * t.n[0] + t.n[1] * t.n[1] + t.n[2] * t.n[2]); }
 
@@ -156,16 +326,52 @@ struct AdaptImpl {
     std::vector<uint8_t> dirty;           // device record out of date
     std::vector<int32_t> dirty_list;
     std::vector<int32_t> trace;
-    LibcRand rng;
+    RandStream rng;
     long long steps = 0;
     bool done = false;
-    Cnt hc = {0, 0, 0, 0, 0, 0, 0, 0};    // host-side walks
+    Cnt hc = {0, 0, 0, 0, 0, 0, 0, 0};    // host-side walks, and the device sample points used
     long long samples = 0, splits = 0, pre_used = 0, host_points = 0;
     uint32_t step_id = 1;
 
+    // Sample points on the device.  Per step: the delta-FF test of every
+    // receiver (ntask), its exclusive scan (toff: the first sample point of
+    // each receiver), and a speculation -- the sample points of tasks
+    // [sp_start, sp_end) drawn from rand() triples sp_base + (t - sp_start).
+    // The host uses a receiver's speculated values only when its draws start
+    // at exactly that triple; a sample loop that breaks early or a rewritten
+    // receiver that draws moves the stream, and the next receiver that samples
+    // starts a new speculation from its own position.
+    uint8_t* d_open = nullptr;
+    uint8_t* h_open = nullptr;            // pinned
+    long long *d_ntask = nullptr, *d_toff = nullptr, *d_tiles = nullptr;
+    long long* h_toff = nullptr;          // pinned, cap + 1
+    unsigned* d_nsplit = nullptr;
+    unsigned* h_nsplit = nullptr;         // pinned
+    T* h_sff = nullptr;                   // mapped: sample point form factors, by task
+    int* h_scode = nullptr;               // mapped: their walk counters
+    T* dm_sff = nullptr;
+    int* dm_scode = nullptr;
+    long long task_cap = 1 << 21;
+    int32_t* d_ring = nullptr;            // rand() values, value i at i % ring_len
+    int32_t* h_ring = nullptr;            // pinned staging of the ring
+    long long ring_len = 1 << 21, ring_hi = 0;
+    long long sp_start = 0, sp_end = 0, sp_base = 0;
+    long long dev_samples = 0, spec_launches = 0, split_candidates = 0;
+    std::vector<void*> pinned;
+
     ~AdaptImpl() {
+        if (stream) cudaStreamSynchronize(stream);
         for (void* p : allocs) cudaFree(p);
+        for (void* p : pinned) cudaFreeHost(p);
         if (stream) cudaStreamDestroy(stream);
+    }
+    template <typename U>
+    int host_alloc(U** p, size_t count, unsigned flags) {
+        void* q = nullptr;
+        CU(cudaHostAlloc(&q, std::max<size_t>(count * sizeof(U), 16), flags));
+        pinned.push_back(q);
+        *p = (U*)q;
+        return RAD_OK;
     }
     template <typename U>
     int alloc(U** p, size_t count) {
@@ -247,12 +453,67 @@ int adapt_create(Scene<T>& s, const Octree<T>& o, const rad_options& opt, int de
         (rc = a.alloc(&a.d_ff, (size_t)a.cap * 4)) || (rc = a.alloc(&a.d_sh, 1)) || (rc = a.alloc(&a.d_state, 1)))
         return rc;
     CU(cudaMemsetAsync(a.d_state, 0, sizeof(State), a.stream));
+    // the sample-point speculation: per-slot test results and offsets, the
+    // rand() ring, and the mapped host buffers the sample kernel writes
+    const int tiles = (a.cap + kScanTile - 1) / kScanTile;
+    if ((rc = a.alloc(&a.d_open, (size_t)a.cap)) || (rc = a.alloc(&a.d_ntask, (size_t)a.cap)) ||
+        (rc = a.alloc(&a.d_toff, (size_t)a.cap + 1)) || (rc = a.alloc(&a.d_tiles, (size_t)tiles)) ||
+        (rc = a.alloc(&a.d_nsplit, 1)) || (rc = a.alloc(&a.d_ring, (size_t)a.ring_len)) ||
+        (rc = a.host_alloc(&a.h_open, (size_t)a.cap, cudaHostAllocDefault)) ||
+        (rc = a.host_alloc(&a.h_toff, (size_t)a.cap + 1, cudaHostAllocDefault)) ||
+        (rc = a.host_alloc(&a.h_nsplit, 1, cudaHostAllocDefault)) ||
+        (rc = a.host_alloc(&a.h_ring, (size_t)a.ring_len, cudaHostAllocDefault)) ||
+        (rc = a.host_alloc(&a.h_sff, (size_t)a.task_cap, cudaHostAllocMapped)) ||
+        (rc = a.host_alloc(&a.h_scode, (size_t)a.task_cap, cudaHostAllocMapped)))
+        return rc;
+    CU(cudaHostGetDevicePointer((void**)&a.dm_sff, a.h_sff, 0));
+    CU(cudaHostGetDevicePointer((void**)&a.dm_scode, a.h_scode, 0));
     a.ff.assign((size_t)a.cap * 4, (T)0);
     a.mod_step.assign((size_t)a.cap, 0);
     a.dirty.assign((size_t)a.cap, 0);
     for (int32_t i = 0; i < s.trinum; i++) a.mark(i);
     a.step_id = 1;
     return adapt_upload_dirty(a);
+}
+
+// keep the device ring holding rand() values [pos, pos + ring_len)
+template <typename T>
+int ring_top_up(AdaptImpl<T>& a) {
+    const long long want = a.rng.pos + a.ring_len;
+    if (a.ring_hi >= want) return RAD_OK;
+    const long long lo = std::max(a.ring_hi, a.rng.pos);
+    for (long long i = lo; i < want; i++) a.h_ring[i % a.ring_len] = a.rng.at(i);
+    // one or two contiguous pieces of the ring
+    long long i = lo;
+    while (i < want) {
+        const long long off = i % a.ring_len;
+        const long long len = std::min(want - i, a.ring_len - off);
+        CU(cudaMemcpyAsync(a.d_ring + off, a.h_ring + off, (size_t)len * 4, cudaMemcpyHostToDevice, a.stream));
+        i += len;
+    }
+    a.ring_hi = want;
+    return RAD_OK;
+}
+
+// enqueue the sample points of tasks [start, ...) drawn from triples base, ...
+// (clipped to the task capacity, the ring and, on the device, the step's total)
+template <typename T>
+int spec_enqueue(AdaptImpl<T>& a, const Slots<T>& S, int n0, long long start, long long base, long long end) {
+    int rc;
+    if ((rc = ring_top_up(a))) return rc;
+    end = std::min(end, a.task_cap);
+    end = std::min(end, start + (a.rng.pos + a.ring_len) / 3 - base);
+    a.sp_start = start;
+    a.sp_base = base;
+    a.sp_end = std::max(start, end);
+    a.spec_launches++;
+    if (a.sp_end <= start || n0 <= 0) return RAD_OK;
+    const long long work = a.sp_end - start;
+    const int blocks = (int)std::max<long long>(1, std::min<long long>((work + 127) / 128, 152 * 16));
+    k_adapt_samples<T><<<blocks, 128, 0, a.stream>>>(S, a.Gd, a.d_sh, a.d_toff, n0, start, a.sp_end, base, a.d_ring,
+                                                     a.ring_len, a.dm_sff, a.dm_scode);
+    CU(cudaGetLastError());
+    return RAD_OK;
 }
 
 template <typename T>
@@ -279,9 +540,34 @@ template <typename T>
 struct StepCtx {
     AdaptImpl<T>& a;
     int src, logsrc, n0;
+    Slots<T> S;               // the device slots as the step started
     bool shooter_changed = false;
+    int err = RAD_OK;
     Shooter<T> sh;            // the shooter as the precompute saw it
     Shooter<T> live;          // rebuilt from the slot after a split rewrote it
+
+    // The device's form factors of receiver d's n sample points, when they are
+    // the ones it draws now: d is unchanged this step (pre_ok), the device's
+    // test gave it n points, and the speculation covering them starts them at
+    // the stream's current triple.  Otherwise a new speculation starts at d.
+    // Null when d's points are evaluated on the host.
+    const T* device_points(int d, int n, const int** codes) {
+        if (a.rng.pos % 3 != 0) return nullptr;
+        const long long t0 = a.h_toff[d];
+        if (a.h_toff[d + 1] - t0 != n) return nullptr;
+        const long long cur = a.rng.pos / 3;
+        auto covered = [&]() {
+            return t0 >= a.sp_start && t0 + n <= a.sp_end && a.sp_base + (t0 - a.sp_start) == cur;
+        };
+        if (!covered()) {
+            int rc = spec_enqueue(a, S, n0, t0, cur, a.h_toff[n0]);
+            if (!rc && cudaStreamSynchronize(a.stream) != cudaSuccess) rc = fail(RAD_ERR_CUDA, "sample-point kernel failed");
+            if (rc) { err = rc; return nullptr; }
+            if (!covered()) return nullptr;
+        }
+        *codes = a.h_scode + t0;
+        return a.h_sff + t0;
+    }
 
     // AdaptCalFF(CalFF(...)) for point p of receiver d (its normal) with ban logdes
     T ff_host(int d, const T* p, int logdes) {
@@ -315,16 +601,26 @@ struct StepCtx {
         T dff;
         if ((dff = (T)std::fabs((double)(ground - ffs))) < o.delta_ff) {
             const int n = (int)(des.area / o.sample_area);
+            const int* codes = nullptr;
+            const T* dev = pre && n > 0 ? device_points(d, n, &codes) : nullptr;
             for (int k = 0; k < n; k++) {
                 // GetPointInTriangle, shade.cpp:49-68
                 T r1 = (T)a.rng.next(), r2 = (T)a.rng.next(), r3 = (T)a.rng.next();
                 const T tot = r1 + r2 + r3;
                 r1 /= tot; r2 /= tot; r3 /= tot;
-                T pt[3];
-                for (int q = 0; q < 3; q++) pt[q] = r1 * des.p[0][q] + r2 * des.p[1][q] + r3 * des.p[2][q];
                 ground = r1 * f[0] + r2 * f[1] + r3 * f[2];
                 a.samples++;
-                ffs = ff_host(d, pt, logdes);
+                if (dev) {      // drawn from this very triple on the device
+                    ffs = dev[k];
+                    a.hc.rays += codes[k] & 0xff;
+                    a.hc.capped += (codes[k] >> 8) & 0xff;
+                    a.hc.loops += (codes[k] >> 16) & 0xff;
+                    a.dev_samples++;
+                } else {
+                    T pt[3];
+                    for (int q = 0; q < 3; q++) pt[q] = r1 * des.p[0][q] + r2 * des.p[1][q] + r3 * des.p[2][q];
+                    ffs = ff_host(d, pt, logdes);
+                }
                 if ((dff = (T)std::fabs((double)(ground - ffs))) > o.delta_ff) break;
             }
             if (dff < o.delta_ff) { deposit(s.slots[src], des, f); return 0; }
@@ -369,18 +665,46 @@ int adapt_step(AdaptImpl<T>& a) {
     a.trace.push_back(src);
     int rc;
     if ((rc = adapt_upload_dirty(a))) return rc;
-    StepCtx<T> cx{a, src, s.slots[src].parent, s.trinum};
+    const int n0 = s.trinum;
+    const Slots<T> S{n0, a.d_vtx, a.d_nrm, a.d_ctr, a.d_frgb, nullptr, nullptr};
+    StepCtx<T> cx{a, src, s.slots[src].parent, n0, S};
     host_shooter(s.slots[src], src, cx.logsrc, cx.sh);
-    // every slot's corner and centre form factors against this shooter
     CU(cudaMemcpyAsync(a.d_sh, &cx.sh, sizeof cx.sh, cudaMemcpyHostToDevice, a.stream));
-    const Slots<T> S{cx.n0, a.d_vtx, a.d_nrm, a.d_ctr, a.d_frgb, nullptr, nullptr};
-    if (cx.n0 > 0) {
-        const int blocks = (int)std::min<long long>((4LL * cx.n0 + 255) / 256, 152 * 16);
-        k_adapt_ff<T><<<blocks, 256, 0, a.stream>>>(S, a.Gd, a.d_sh, cx.n0, a.d_ff, a.d_state);
+    a.h_toff[0] = 0;
+    a.sp_start = a.sp_end = a.sp_base = 0;
+    if (n0 > 0) {
+        // the receivers the loop will visit, as the step starts
+        for (int d = 0; d < n0; d++) {
+            const Slot<T>& t = s.slots[d];
+            a.h_open[d] = d != src && t.parent >= 0 && is_open(t);
+        }
+        CU(cudaMemcpyAsync(a.d_open, a.h_open, (size_t)n0, cudaMemcpyHostToDevice, a.stream));
+        CU(cudaMemsetAsync(a.d_nsplit, 0, sizeof(unsigned), a.stream));
+        // every slot's corner and centre form factors against this shooter
+        const int blocks = (int)std::min<long long>((4LL * n0 + 255) / 256, 152 * 16);
+        k_adapt_ff<T><<<blocks, 256, 0, a.stream>>>(S, a.Gd, a.d_sh, n0, a.d_ff, a.d_state);
+        // the delta-FF test of every receiver, and its sample points numbered
+        const rad_options& o = s.opt;
+        k_adapt_test<T><<<(n0 + 255) / 256, 256, 0, a.stream>>>(S, n0, a.d_ff, a.d_open, o.adapt_area, o.delta_ff,
+                                                              o.sample_area, pool_full(s, 4) ? 1 : 0, a.d_ntask,
+                                                              a.d_nsplit);
+        const int tiles = (n0 + kScanTile - 1) / kScanTile;
+        k_scan_tiles<<<tiles, kScanTile, 0, a.stream>>>(a.d_ntask, n0, a.d_toff, a.d_tiles);
+        k_scan_sums<<<1, kScanTile, 0, a.stream>>>(a.d_tiles, tiles, a.d_toff, n0);
+        k_scan_add<<<tiles, kScanTile, 0, a.stream>>>(a.d_tiles, n0, a.d_toff);
         CU(cudaGetLastError());
-        CU(cudaMemcpyAsync(a.ff.data(), a.d_ff, (size_t)cx.n0 * 4 * sizeof(T), cudaMemcpyDeviceToHost, a.stream));
+        // the first speculation: every sample point of the step, as if none broke early
+        int rc0;
+        if (a.rng.pos % 3 == 0 && (rc0 = spec_enqueue(a, S, n0, 0, a.rng.pos / 3, a.task_cap))) return rc0;
+        CU(cudaMemcpyAsync(a.ff.data(), a.d_ff, (size_t)n0 * 4 * sizeof(T), cudaMemcpyDeviceToHost, a.stream));
+        CU(cudaMemcpyAsync(a.h_toff, a.d_toff, (size_t)(n0 + 1) * sizeof(long long), cudaMemcpyDeviceToHost, a.stream));
+        CU(cudaMemcpyAsync(a.h_nsplit, a.d_nsplit, sizeof(unsigned), cudaMemcpyDeviceToHost, a.stream));
     }
     CU(cudaStreamSynchronize(a.stream));
+    if (n0 > 0) {
+        a.sp_end = std::min(a.sp_end, a.h_toff[n0]);
+        a.split_candidates += *a.h_nsplit;
+    }
     // serialRadiosity's receiver loop, rad.cpp:464-485 (bound re-read: splits append slots)
     for (int d = 0; d < s.trinum; d++) {
         if (d == src) continue;
@@ -388,6 +712,7 @@ int adapt_step(AdaptImpl<T>& a) {
         if (t.parent < 0) continue;
         if (!is_open(t)) continue;
         if (cx.shade(d, t.parent)) d--;
+        if (cx.err) return cx.err;
     }
     Slot<T>& sr = s.slots[src];
     sr.deltaB[0] = sr.deltaB[1] = sr.deltaB[2] = 0;
@@ -482,6 +807,18 @@ int rad_adapt_stats(const rad_adapt* h, rad_stats* st, int64_t* host_points, int
         if (host_points) *host_points = a.host_points;
         if (splits) *splits = a.splits;
         if (samples) *samples = a.samples;
+        return RAD_OK;
+    };
+    return h->a32 ? go(*h->a32) : go(*h->a64);
+}
+
+int rad_adapt_device_stats(const rad_adapt* h, int64_t* device_points, int64_t* speculations,
+                           int64_t* split_candidates) {
+    if (!h) return fail(RAD_ERR_ARG, "rad_adapt_device_stats: null handle");
+    auto go = [&](auto& a) {
+        if (device_points) *device_points = a.dev_samples;
+        if (speculations) *speculations = a.spec_launches;
+        if (split_candidates) *split_candidates = a.split_candidates;
         return RAD_OK;
     };
     return h->a32 ? go(*h->a32) : go(*h->a64);

@@ -53,21 +53,12 @@ namespace dev {
 // Several shooters per step keep the separate k_setup.
 // a group is split in the next step when its item took longer than this
 // fraction of the step (an item that was already split: the second figure)
-#ifndef RAD_HEAVY_FRAC
-#define RAD_HEAVY_FRAC 0.55
-#endif
-#ifndef RAD_HEAVY_FRAC_SPLIT
-#define RAD_HEAVY_FRAC_SPLIT 0.27
-#endif
+constexpr double kHeavyFrac = 0.55, kHeavyFracSplit = 0.27;
 // ... and longer than this multiple of the step's mean group time
-#ifndef RAD_HEAVY_MEAN_MULT
-#define RAD_HEAVY_MEAN_MULT 2.5
-#endif
+constexpr double kHeavyMeanMult = 2.5;
 // a group shot whole that took longer than this multiple of the step's mean
 // group time starts early in the next step
-#ifndef RAD_EARLY_MEAN_MULT
-#define RAD_EARLY_MEAN_MULT 1.5
-#endif
+constexpr double kEarlyMeanMult = 1.5;
 // Two forms of the single-shooter kernel, picked per scene (layout):
 //   1 (tail-bound: a step is about one wave of groups) -- 3 CTAs per SM, 80
 //     registers, a split group's items cast each corner with 4 lanes that
@@ -147,13 +138,18 @@ k_shoot(Slots<T> S, Grid<T> G, Shooter<T>* shooters, State* st, Partial* __restr
         }
         // one call site when every item is cast one lane per corner: the
         // walk is inlined once, which keeps the register count down
+        // FUSED: at most one shooter per step.  One-lane items then re-read
+        // the deposit's inputs after the walk instead of holding them in
+        // registers (ONE); measured 3-4% faster in form 2 and in the batched
+        // kernel, while the 4-lane items of form 1 measured 20-25% slower
+        // that way, so they keep the registers.
         if constexpr (HL == 1 || COUNT) {
-            shoot_item<T, COUNT, 1>(S, Gs, sh, nsh, i0, n_item, lane, conv, kk, ks, c);
+            shoot_item<T, COUNT, 1, FUSED>(S, Gs, sh, nsh, i0, n_item, lane, conv, kk, ks, c);
         } else {
             if (g < n_heavy_items)
-                shoot_item<T, false, HL>(S, Gs, sh, nsh, i0, n_item, lane, conv, kk, ks, c);
+                shoot_item<T, false, HL, false>(S, Gs, sh, nsh, i0, n_item, lane, conv, kk, ks, c);
             else
-                shoot_item<T, COUNT, 1>(S, Gs, sh, nsh, i0, n_item, lane, conv, kk, ks, c);
+                shoot_item<T, COUNT, 1, FUSED>(S, Gs, sh, nsh, i0, n_item, lane, conv, kk, ks, c);
         }
         if (split && lane == 0) {
             const long long dt = (long long)(global_ns() - t_item);
@@ -254,7 +250,6 @@ __global__ void __launch_bounds__(kSetupThreads)
 k_setup(Slots<T> S, Shooter<T>* shooters, State* st, const Partial* __restrict__ part, int nparts, T conv, int P) {
     __shared__ unsigned long long bk[kSetupThreads / 32];
     __shared__ int bs[kSetupThreads / 32];
-    __shared__ int bc[kSetupThreads / 32];
     __shared__ int chosen[kMaxShooters];
     __shared__ int nch;
     if (st->done || st->paused) return;
@@ -281,47 +276,10 @@ k_setup(Slots<T> S, Shooter<T>* shooters, State* st, const Partial* __restrict__
         }
         __syncthreads();
     } else {
-        // listCanditate for P > 1: n = min((|C|+4)/5, P) largest (key, slot)
-        // pairs, descending; one block-wide argmax per rank
-        unsigned long long lim_k = ~0ull;
-        int lim_s = 0x7fffffff;
-        int n_take = 0;
-        for (int rank = 0; rank < P; rank++) {
-            unsigned long long kk = 0;
-            int ks = -1, cnt = 0;
-            for (int i = threadIdx.x; i < S.n; i += blockDim.x) {
-                const Q4<T> fr = S.frgb[i];
-                if ((int)fr.w < 0) continue;
-                const Q4<T> db = S.deltaB[i];
-                const T key = (db.x + db.y) + db.z;
-                if (!(key > conv)) continue;
-                const unsigned long long o = key_order(key);
-                cnt++;
-                if (part_less(o, i, lim_k, lim_s) && part_less(kk, ks, o, i)) { kk = o; ks = i; }
-            }
-            warp_max(kk, ks);
-            cnt = __reduce_add_sync(kFull, cnt);
-            if (lane == 0) { bk[wid] = kk; bs[wid] = ks; bc[wid] = cnt; }
-            __syncthreads();
-            if (wid == 0) {
-                kk = bk[lane];
-                ks = bs[lane];
-                int cc = __reduce_add_sync(kFull, bc[lane]);
-                warp_max(kk, ks);
-                if (lane == 0) {
-                    if (rank == 0) nch = min((cc + 4) / 5, P);
-                    chosen[rank] = ks;
-                    bk[0] = kk;
-                    bs[0] = ks;
-                }
-            }
-            __syncthreads();
-            lim_k = bk[0];
-            lim_s = bs[0];
-            n_take = nch;
-            __syncthreads();
-            if (rank + 1 >= n_take) break;
-        }
+        // listCanditate for P > 1: the n = min((|C|+4)/5, P) largest pairs
+        const int n = cta_top_shooters(S, conv, P, chosen);
+        if (threadIdx.x == 0) nch = n;
+        __syncthreads();
     }
     const int n = nch;
     if (n == 0) {
@@ -376,38 +334,6 @@ __global__ void k_unshot_total(const double* part, int n, double* out) {
     if (threadIdx.x == 0) *out = t;
 }
 
-// ------------------------------------------------------------------ upload
-// The cell table and the list records are expanded on the device from
-// compact host arrays: a leaf index per cell, and per triangle one record
-// group gathered for each list entry naming it.  The records are the ones
-// pack_scene writes (the batched and adaptive forms still pack on the host).
-template <typename T>
-__global__ void k_expand_cells(const int32_t* __restrict__ cell_leaf, const T* __restrict__ leaf_box,
-                               const int32_t* __restrict__ leaf_range, long long n_cell, CellRec<T>* __restrict__ out) {
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n_cell;
-         i += (long long)gridDim.x * blockDim.x) {
-        const int l = cell_leaf[i];
-        const T* b = leaf_box + (size_t)l * 8;
-        CellRec<T> r;
-        r.h = make_int4(l, leaf_range[2 * l], leaf_range[2 * l + 1], 0);
-        r.a = {b[0], b[1], b[2], b[4]};
-        r.b = {b[5], b[6], 0, 0};
-        out[i] = r;
-    }
-}
-
-// entry k = the five records of triangle entry_tri[k]
-template <typename T>
-__global__ void k_gather_entries(const int32_t* __restrict__ entry_tri, const Q4<T>* __restrict__ tri_rec,
-                                 long long n_ent, Q4<T>* __restrict__ out) {
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n_ent * 5;
-         i += (long long)gridDim.x * blockDim.x) {
-        const long long k = i / 5;
-        const int j = (int)(i - 5 * k);
-        out[i] = tri_rec[(size_t)entry_tri[k] * 5 + j];
-    }
-}
-
 // ------------------------------------------------------------------ queries
 template <typename T>
 __global__ void k_ray_hit(Grid<T> G, const T* __restrict__ p, const T* __restrict__ v, const int* __restrict__ ban,
@@ -450,6 +376,9 @@ __global__ void k_form_factors(Slots<T> S, Grid<T> G, const Shooter<T>* __restri
 // serves both precisions.
 constexpr int kNoAllocMaxShooters = 64;
 static __device__ __align__(256) unsigned char g_noalloc_shooters[kNoAllocMaxShooters * sizeof(Shooter<double>)];
+static_assert(sizeof(Shooter<float>) <= sizeof(Shooter<double>) && alignof(Shooter<double>) <= 256 &&
+                  alignof(Shooter<float>) <= 256,
+              "the fixed array holds 64 records of either precision");
 
 struct ShooterSlots { int slot[kNoAllocMaxShooters]; };
 
@@ -526,6 +455,7 @@ struct DevImpl : DevBase {
     cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
     std::vector<void*> allocs;
     size_t bytes = 0;
+    long long h2d_bytes = 0;   // host -> device copies of the upload
     State host{};   // mirror after the last synchronisation
 
     ~DevImpl() override {
@@ -600,6 +530,7 @@ int upload(const Scene<T>& s, const Octree<T>& o, const rad_options& opt, int de
         int r = d.alloc(dst, src.size());
         if (r) return r;
         CU(cudaMemcpyAsync(*dst, src.data(), src.size() * sizeof(src[0]), cudaMemcpyHostToDevice, d.stream));
+        d.h2d_bytes += (long long)(src.size() * sizeof(src[0]));
         return RAD_OK;
     };
     const long long n_cell = (long long)o.cell_leaf.size(), n_ent = (long long)o.entry_tri.size();
@@ -674,12 +605,13 @@ int upload(const Scene<T>& s, const Octree<T>& o, const rad_options& opt, int de
     st.early = d_early;
     st.estamp = d_estamp;
     st.early_ns = 0x7fffffffffffffffLL;
-    st.frac = RAD_HEAVY_FRAC;
-    st.frac_split = RAD_HEAVY_FRAC_SPLIT;
-    st.mean_mult = RAD_HEAVY_MEAN_MULT;
-    st.early_mult = RAD_EARLY_MEAN_MULT;
+    st.frac = kHeavyFrac;
+    st.frac_split = kHeavyFracSplit;
+    st.mean_mult = kHeavyMeanMult;
+    st.early_mult = kEarlyMeanMult;
     st.t_start = ~0ull;
     CU(cudaMemcpyAsync(d.d_state, &st, sizeof st, cudaMemcpyHostToDevice, d.stream));
+    d.h2d_bytes += (long long)sizeof st;
     CU(cudaMemsetAsync(d.d_shooters, 0, sizeof(Shooter<T>) * d.P, d.stream));
     CU(cudaMemsetAsync(d.d_part, 0, sizeof(Partial) * std::max(d.n_cta1, d.n_cta2), d.stream));
     // initial selection keys: a step with no shooter only reduces the keys
@@ -923,7 +855,16 @@ int form_factors_noalloc(DevImpl<T>& d, const int32_t* src, int n_src, const int
         if (src[j] < 0 || src[j] >= d.S.n) return fail(RAD_ERR_ARG, "shooter slot out of range");
         slots.slot[j] = src[j];
     }
-    CU(cudaSetDevice(d.device));
+    // the handle's device is made current for the launches; the caller's
+    // current device is restored on every path out
+    int caller_dev = 0;
+    CU(cudaGetDevice(&caller_dev));
+    struct Restore {
+        int dev;
+        bool on;
+        ~Restore() { if (on) cudaSetDevice(dev); }
+    } restore{caller_dev, caller_dev != d.device};
+    if (caller_dev != d.device) CU(cudaSetDevice(d.device));
     void* scratch = nullptr;
     int rc = noalloc_scratch(d.device, &scratch);
     if (rc) return rc;
@@ -1045,6 +986,7 @@ int rad_dev_stats(const rad_dev* h, rad_stats* st) {
         st->converged = d.host.done;
         st->n_slots = d.S.n;
         st->device_bytes = (int64_t)(d.bytes + d.trace_cap * 4);
+        st->h2d_bytes = (int64_t)d.h2d_bytes;
         using TT = typename std::remove_reference<decltype(d)>::type::Real;
         k_unshot<TT><<<kUnshotCtas, kUnshotThreads, 0, d.stream>>>(d.S, d.d_unshot);
         k_unshot_total<<<1, 32, 0, d.stream>>>(d.d_unshot, kUnshotCtas, d.d_unshot + kUnshotCtas);

@@ -7,7 +7,11 @@
 #pragma once
 
 #include <cstdint>
+#include <cstdlib>
+#include <new>
 #include <string>
+#include <type_traits>
+#include <utility>
 #include <vector>
 
 #include "rad_gb300.h"
@@ -39,9 +43,35 @@ struct Slot {
     int32_t nb[3];
 };
 
+// Allocator of the slot pool: memory from calloc, and value-initialisation
+// that writes nothing, so a pool sized to the -triangle limit (the
+// reference's static TriStore of 10^6 slots, rad.h:9) reads as zeros without
+// being written -- the operating system maps zero pages as they are first
+// touched.  Only for trivially copyable records in vectors that never shrink
+// and grow again in place.
+template <typename U>
+struct ZeroPages {
+    using value_type = U;
+    ZeroPages() = default;
+    template <typename V> ZeroPages(const ZeroPages<V>&) {}
+    U* allocate(std::size_t n) {
+        void* p = std::calloc(n ? n : 1, sizeof(U));
+        if (!p) throw std::bad_alloc();
+        return static_cast<U*>(p);
+    }
+    void deallocate(U* p, std::size_t) { std::free(p); }
+    template <typename V, typename... A>
+    void construct(V* p, A&&... a) {
+        if constexpr (sizeof...(A) > 0) ::new ((void*)p) V(std::forward<A>(a)...);
+    }
+    template <typename V> bool operator==(const ZeroPages<V>&) const { return true; }
+    template <typename V> bool operator!=(const ZeroPages<V>&) const { return false; }
+};
+
 template <typename T>
 struct Scene {
-    std::vector<Slot<T>> slots;   // pool, zero-filled; [0, trinum) live
+    static_assert(std::is_trivially_copyable<Slot<T>>::value, "slots are plain records");
+    std::vector<Slot<T>, ZeroPages<Slot<T>>> slots;   // pool, zero-filled; [0, trinum) live
     int32_t trinum = 0;           // live slots
     int32_t n_orig = 0;           // triangles read from the input (the octree indexes these)
     T G0[3] = {0, 0, 0};

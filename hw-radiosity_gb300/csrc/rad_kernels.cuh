@@ -622,7 +622,7 @@ __device__ __forceinline__ void flush_counters(State* st, Cnt& c, int lane) {
 // The deposit is the same for every layout: the three corners' form factors
 // meet by shuffle, the group's lane 0 writes its corner's accB, and corner 0's
 // lane 0 keeps the slot's deltaB in the reference's order.
-template <typename T, bool COUNT, int L>
+template <typename T, bool COUNT, int L, bool ONE = false>
 __device__ __forceinline__ void shoot_item(const Slots<T>& S, const Grid<T>& G, const Shooter<T>* sh, int nsh, int i0,
                                            int n_item, int lane, T conv, unsigned long long& kk, int& ks, Cnt& c) {
     static_assert(L == 1 || !COUNT, "the counting pass uses the serial walk");
@@ -648,6 +648,56 @@ __device__ __forceinline__ void shoot_item(const Slots<T>& S, const Grid<T>& G, 
     const int base = 3 * L * min(r, n_item - 1);   // lane 0 of corner 0 of slot r
     const bool open = (((ballot >> base) | (ballot >> (base + L)) | (ballot >> (base + 2 * L))) & 1u) != 0;
     const bool active = live && !is_src && open && nsh > 0;
+    if (ONE) {
+        // one shooter: the deposit's inputs are read again after the walk
+        // (the warp owns the slot, so they are unchanged) instead of being
+        // held in registers across it
+        T ff = 0;
+        if (active) {
+            const Q4<T> pp = S.vtx[i * 3 + v];
+            const Q4<T> nn = S.nrm[i];
+            const T pv[3] = {pp.x, pp.y, pp.z}, nd[3] = {nn.x, nn.y, nn.z};
+            if constexpr (L == 1)
+                ff = corner_ff<T, COUNT>(sh[0], pv, nd, nn.w, parent, G, c);
+            else
+                ff = corner_ff_lanes<T, L>(sh[0], pv, nd, nn.w, parent, sub, gmask, G, c);
+        }
+        const T f0 = shfl(ff, base), f1 = shfl(ff, base + L), f2 = shfl(ff, base + 2 * L);
+        T d0 = 0, d1 = 0, d2 = 0;
+        if (live && v == 0) { db = S.deltaB[i]; d0 = db.x; d1 = db.y; d2 = db.z; }
+        if (active) {
+            fr = S.frgb[i];
+            acc = S.accB[i * 3 + v];
+            const T k = (T)(0.5 / 255.0);   // RefRatio / 255.0, shade.cpp:246
+            const T lo0 = fr.x * k * sh[0].deltaB[0] / 3;
+            const T lo1 = fr.y * k * sh[0].deltaB[1] / 3;
+            const T lo2 = fr.z * k * sh[0].deltaB[2] / 3;
+            T a0 = acc.x, a1 = acc.y, a2 = acc.z;
+            a0 += lo0 * ff; a1 += lo1 * ff; a2 += lo2 * ff;
+            if (v == 0) {
+                d0 += lo0 * f0; d0 += lo0 * f1; d0 += lo0 * f2;
+                d1 += lo1 * f0; d1 += lo1 * f1; d1 += lo1 * f2;
+                d2 += lo2 * f0; d2 += lo2 * f1; d2 += lo2 * f2;
+            }
+            if (lead) {
+                Q4<T> o = {a0, a1, a2, acc.w};
+                S.accB[i * 3 + v] = o;
+                if (v == 0) { Q4<T> q = {d0, d1, d2, db.w}; S.deltaB[i] = q; }
+            }
+        }
+        if (live && is_src && v == 0) {       // rad.cpp:446-449
+            d0 = d1 = d2 = 0;
+            if (lead) { Q4<T> q = {0, 0, 0, db.w}; S.deltaB[i] = q; }
+        }
+        if (live && v == 0 && lead) {
+            const T key = (d0 + d1) + d2;
+            if (key > conv) {
+                const unsigned long long o = key_order(key);
+                if (part_less(kk, ks, o, i)) { kk = o; ks = i; }
+            }
+        }
+        return;
+    }
     if (live && v == 0) db = S.deltaB[i];
 
     T pv[3] = {0, 0, 0}, nd[3] = {0, 0, 0}, ndlen = 1;
@@ -702,10 +752,10 @@ __device__ __forceinline__ void shoot_item(const Slots<T>& S, const Grid<T>& G, 
 }
 
 // One 10-slot group in the common layout (lanes 3r+v: corner v of slot g*10+r).
-template <typename T, bool COUNT>
+template <typename T, bool COUNT, bool ONE = false>
 __device__ __forceinline__ void shoot_group(const Slots<T>& S, const Grid<T>& G, const Shooter<T>* sh, int nsh,
                                             int g, int lane, T conv, unsigned long long& kk, int& ks, Cnt& c) {
-    shoot_item<T, COUNT, 1>(S, G, sh, nsh, g * kSlotsPerWarp, kSlotsPerWarp, lane, conv, kk, ks, c);
+    shoot_item<T, COUNT, 1, ONE>(S, G, sh, nsh, g * kSlotsPerWarp, kSlotsPerWarp, lane, conv, kk, ks, c);
 }
 
 // Shooter record for slot `slot`: normal, |n|, centre, area, unshot energy,
@@ -760,6 +810,90 @@ __device__ void build_shooter(const Slots<T>& S, int slot, Shooter<T>& s) {
     make_shooter(p, c, n, nn.w, cc.w, d, slot, (int)fr.w, s);
 }
 
+
+// listCanditate (rad.cpp:387-404) over one scene's slots, by one CTA of at
+// most 1024 threads: the n = min((|C|+4)/5, P) largest (key, slot) pairs,
+// descending (ties: higher slot first), where C is the set of live slots whose
+// key (dB0 + dB1) + dB2 exceeds conv.  One block-wide argmax per rank, each
+// below the previous rank's pair.  chosen (shared, >= P entries) receives the
+// slots; returns n (0: converged).  Every thread gets the same n.
+template <typename T>
+__device__ int cta_top_shooters(const Slots<T>& S, T conv, int P, int* chosen) {
+    __shared__ unsigned long long bk[32];
+    __shared__ int bs[32], bc[32];
+    __shared__ int nch;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+    unsigned long long lim_k = ~0ull;
+    int lim_s = 0x7fffffff;
+    for (int rank = 0; rank < P; rank++) {
+        unsigned long long kk = 0;
+        int ks = -1, cnt = 0;
+        for (int i = threadIdx.x; i < S.n; i += blockDim.x) {
+            const Q4<T> fr = S.frgb[i];
+            if ((int)fr.w < 0) continue;
+            const Q4<T> db = S.deltaB[i];
+            const T key = (db.x + db.y) + db.z;
+            if (!(key > conv)) continue;
+            const unsigned long long o = key_order(key);
+            cnt++;
+            if (part_less(o, i, lim_k, lim_s) && part_less(kk, ks, o, i)) { kk = o; ks = i; }
+        }
+        warp_max(kk, ks);
+        cnt = __reduce_add_sync(kFull, cnt);
+        if (lane == 0) { bk[wid] = kk; bs[wid] = ks; bc[wid] = cnt; }
+        __syncthreads();
+        if (wid == 0) {
+            kk = lane < nw ? bk[lane] : 0;
+            ks = lane < nw ? bs[lane] : -1;
+            const int cc = __reduce_add_sync(kFull, lane < nw ? bc[lane] : 0);
+            warp_max(kk, ks);
+            if (lane == 0) {
+                if (rank == 0) nch = min((cc + 4) / 5, P);
+                chosen[rank] = ks;
+                bk[0] = kk;
+                bs[0] = ks;
+            }
+        }
+        __syncthreads();
+        lim_k = bk[0];
+        lim_s = bs[0];
+        const int n_take = nch;
+        __syncthreads();
+        if (rank + 1 >= n_take) break;
+    }
+    return nch;
+}
+
+// ------------------------------------------------------------------ upload
+// The cell table and the list records are expanded on the device from
+// compact host arrays: a leaf index per cell, and per triangle one record
+// group gathered for each list entry naming it.
+template <typename T>
+__global__ void k_expand_cells(const int32_t* __restrict__ cell_leaf, const T* __restrict__ leaf_box,
+                               const int32_t* __restrict__ leaf_range, long long n_cell, CellRec<T>* __restrict__ out) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n_cell;
+         i += (long long)gridDim.x * blockDim.x) {
+        const int l = cell_leaf[i];
+        const T* b = leaf_box + (size_t)l * 8;
+        CellRec<T> r;
+        r.h = make_int4(l, leaf_range[2 * l], leaf_range[2 * l + 1], 0);
+        r.a = {b[0], b[1], b[2], b[4]};
+        r.b = {b[5], b[6], 0, 0};
+        out[i] = r;
+    }
+}
+
+// entry k = the five records of triangle entry_tri[k]
+template <typename T>
+__global__ void k_gather_entries(const int32_t* __restrict__ entry_tri, const Q4<T>* __restrict__ tri_rec,
+                                 long long n_ent, Q4<T>* __restrict__ out) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n_ent * 5;
+         i += (long long)gridDim.x * blockDim.x) {
+        const long long k = i / 5;
+        const int j = (int)(i - 5 * k);
+        out[i] = tri_rec[(size_t)entry_tri[k] * 5 + j];
+    }
+}
 
 // ------------------------------------------------------------------ host packing
 // Device records of one scene, appended to growing host arrays so several

@@ -22,6 +22,7 @@
 #include "capi_internal.h"
 #include "octree_build.h"
 #include "octree_geom.h"
+#include "prep_workspace.h"
 
 namespace radgb {
 namespace dev {
@@ -57,19 +58,15 @@ namespace {
             return fail(RAD_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
     } while (0)
 
-// device buffers that grow by doubling, freed with the builder
+// buffer k of this thread's preparation workspace
 struct DevBuf {
+    PrepWorkspace& ws;
+    size_t k;
     void* p = nullptr;
-    size_t cap = 0;
     int ensure(size_t bytes) {
-        if (bytes <= cap) return RAD_OK;
-        if (p) cudaFree(p);
-        p = nullptr;
-        cap = std::max(bytes, cap * 2);
-        CU(cudaMalloc(&p, cap));
+        CU(ws.buffer(k, bytes, &p));
         return RAD_OK;
     }
-    ~DevBuf() { if (p) cudaFree(p); }
 };
 
 bool is_leaf(size_t n, int level) { return n <= (size_t)kMaxTriPerNode || level >= kMaxLevel; }
@@ -77,9 +74,9 @@ bool is_leaf(size_t n, int level) { return n <= (size_t)kMaxTriPerNode || level 
 template <typename T>
 int build_device(const Scene<T>& s, Octree<T>& o, int device) {
     CU(cudaSetDevice(device));
+    PrepWorkspace& ws = prep_workspace(device);
     cudaStream_t st = nullptr;
-    CU(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
-    struct StreamGuard { cudaStream_t s; ~StreamGuard() { if (s) cudaStreamDestroy(s); } } guard{st};
+    CU(ws.stream(&st));
     const int n = s.n_orig;
     Part<T> P;
     P.min_edge = s.G1[0] - s.G0[0];                       // raycast.cpp:226
@@ -110,7 +107,7 @@ int build_device(const Scene<T>& s, Octree<T>& o, int device) {
     for (int i = 0; i < n; i++)
         for (int v = 0; v < 3; v++)
             for (int k = 0; k < 3; k++) tv[(size_t)i * 9 + v * 3 + k] = s.slots[i].p[v][k];
-    DevBuf d_tv, d_tri, d_node, d_box, d_mask;
+    DevBuf d_tv{ws, 0}, d_tri{ws, 1}, d_node{ws, 2}, d_box{ws, 3}, d_mask{ws, 4};
     if (int rc = d_tv.ensure(tv.size() * sizeof(T))) return rc;
     CU(cudaMemcpyAsync(d_tv.p, tv.data(), tv.size() * sizeof(T), cudaMemcpyHostToDevice, st));
     struct Open { int32_t node; Box<T> box; };

@@ -20,6 +20,7 @@
 #include <vector>
 
 #include "capi_internal.h"
+#include "prep_workspace.h"
 
 namespace radgb {
 namespace dev {
@@ -131,10 +132,6 @@ namespace {
             return fail(RAD_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
     } while (0)
 
-struct Mem {
-    std::vector<void*> p;
-    ~Mem() { for (void* q : p) cudaFree(q); }
-};
 
 template <typename T>
 int link_neighbours_device(Scene<T>& s, int device) {
@@ -152,36 +149,39 @@ int link_neighbours_device(Scene<T>& s, int device) {
     unsigned cap = 1;
     while (cap < 6u * (unsigned)N) cap <<= 1;
     const int nc = 3 * N;
-    Mem m;
+    // this thread's preparation workspace: its stream and buffers 0..6
+    PrepWorkspace& ws = prep_workspace(device);
+    cudaStream_t st = nullptr;
+    CU(ws.stream(&st));
     T *dp, *dn;
     int *table, *head, *next, *err;
     unsigned long long* best;
-    auto get = [&](auto** q, size_t bytes) -> int {
+    auto get = [&](size_t k, auto** q, size_t bytes) -> int {
         void* r = nullptr;
-        CU(cudaMalloc(&r, bytes));
-        m.p.push_back(r);
+        CU(ws.buffer(k, bytes, &r));
         *q = (std::remove_pointer_t<decltype(q)>)r;
         return RAD_OK;
     };
     int rc;
-    if ((rc = get(&dp, hp.size() * sizeof(T))) || (rc = get(&dn, hn.size() * sizeof(T))) ||
-        (rc = get(&table, (size_t)cap * 4)) || (rc = get(&head, (size_t)nc * 4)) || (rc = get(&next, (size_t)nc * 4)) ||
-        (rc = get(&err, 4)) || (rc = get(&best, (size_t)nc * 8)))
+    if ((rc = get(0, &dp, hp.size() * sizeof(T))) || (rc = get(1, &dn, hn.size() * sizeof(T))) ||
+        (rc = get(2, &table, (size_t)cap * 4)) || (rc = get(3, &head, (size_t)nc * 4)) ||
+        (rc = get(4, &next, (size_t)nc * 4)) || (rc = get(5, &err, 4)) || (rc = get(6, &best, (size_t)nc * 8)))
         return rc;
-    CU(cudaMemcpy(dp, hp.data(), hp.size() * sizeof(T), cudaMemcpyHostToDevice));
-    CU(cudaMemcpy(dn, hn.data(), hn.size() * sizeof(T), cudaMemcpyHostToDevice));
-    CU(cudaMemset(table, 0xff, (size_t)cap * 4));
-    CU(cudaMemset(head, 0xff, (size_t)nc * 4));
-    CU(cudaMemset(err, 0, 4));
-    CU(cudaMemset(best, 0, (size_t)nc * 8));
+    CU(cudaMemcpyAsync(dp, hp.data(), hp.size() * sizeof(T), cudaMemcpyHostToDevice, st));
+    CU(cudaMemcpyAsync(dn, hn.data(), hn.size() * sizeof(T), cudaMemcpyHostToDevice, st));
+    CU(cudaMemsetAsync(table, 0xff, (size_t)cap * 4, st));
+    CU(cudaMemsetAsync(head, 0xff, (size_t)nc * 4, st));
+    CU(cudaMemsetAsync(err, 0, 4, st));
+    CU(cudaMemsetAsync(best, 0, (size_t)nc * 8, st));
     const int blocks = (nc + 255) / 256;
-    dev::k_group_corners<T><<<blocks, 256>>>(dp, nc, table, cap - 1, head, next, err);
-    dev::k_link_pairs<T><<<blocks, 256>>>(dp, dn, N, table, head, next, cap - 1, best);
+    dev::k_group_corners<T><<<blocks, 256, 0, st>>>(dp, nc, table, cap - 1, head, next, err);
+    dev::k_link_pairs<T><<<blocks, 256, 0, st>>>(dp, dn, N, table, head, next, cap - 1, best);
     CU(cudaGetLastError());
     std::vector<unsigned long long> hb((size_t)nc);
     int herr = 0;
-    CU(cudaMemcpy(hb.data(), best, hb.size() * 8, cudaMemcpyDeviceToHost));
-    CU(cudaMemcpy(&herr, err, 4, cudaMemcpyDeviceToHost));
+    CU(cudaMemcpyAsync(hb.data(), best, hb.size() * 8, cudaMemcpyDeviceToHost, st));
+    CU(cudaMemcpyAsync(&herr, err, 4, cudaMemcpyDeviceToHost, st));
+    CU(cudaStreamSynchronize(st));
     if (herr) return fail(RAD_ERR_CAPACITY, "neighbour-link table overflow");
     for (int i = 0; i < N; i++)
         for (int v = 0; v < 3; v++) {

@@ -21,19 +21,14 @@ PKG = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 REPO = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 INC = os.path.join(REPO, "include")
-# RAD_BUILD_DIR / RAD_NVCC_EXTRA build a variant (e.g. other launch bounds)
-# into its own directory, for tuning sweeps; the default build is in-tree.
-_VAR = os.environ.get("RAD_BUILD_DIR")
-OBJ = os.path.join(_VAR, "obj") if _VAR else os.path.join(PKG, "_build")
-LIB = os.path.join(_VAR, "lib", "librad_gb300.so") if _VAR else os.path.join(PKG, "lib", "librad_gb300.so")
-BIN = os.path.join(_VAR, "bin", "rad") if _VAR else os.path.join(PKG, "bin", "rad")
+OBJ = os.path.join(PKG, "_build")
+LIB = os.path.join(PKG, "lib", "librad_gb300.so")
+BIN = os.path.join(PKG, "bin", "rad")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 HOST_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-Wno-unused-function", f"-I{INC}"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "--prec-div=true", "--prec-sqrt=true",
                      "-Xcompiler", "-fPIC,-ffp-contract=off", f"-I{INC}", "-Xptxas", "-v"]
-
-NVCC_FLAGS += os.environ.get("RAD_NVCC_EXTRA", "").split()
 
 HOST_SRC = ["scene.cpp", "octree.cpp", "capi.cpp"]
 CUDA_SRC = ["rad_dev.cu", "rad_batch.cu", "rad_adapt.cu", "rad_raster.cu", "rad_octree_dev.cu", "rad_scene_dev.cu"]

@@ -55,7 +55,7 @@ class Stats(C.Structure):
                 ("cells", C.c_int64), ("tri_tests", C.c_int64), ("se_tests", C.c_int64),
                 ("prec_steps", C.c_int64), ("walk_cap_hits", C.c_int64), ("converged", C.c_int32),
                 ("n_slots", C.c_int32), ("device_bytes", C.c_int64), ("walk_loops", C.c_int64),
-                ("unshot_power", C.c_double)]
+                ("unshot_power", C.c_double), ("h2d_bytes", C.c_int64)]
 
 
 class RadError(RuntimeError):
@@ -125,8 +125,12 @@ def load(path: Optional[str] = None) -> C.CDLL:
         "rad_batch_trace": (C.c_int, [vp, i32, vp, i64, P(i64)]),
         "rad_batch_stats": (C.c_int, [vp, P(Stats)]),
         "rad_batch_set_counting": (C.c_int, [vp, i32]),
+        "rad_batch_set_form": (C.c_int, [vp, i32]),
+        "rad_batch_form": (C.c_int, [vp]),
+        "rad_batch_autotune": (C.c_int, [vp, i32, i32, P(i32)]),
         "rad_batch_destroy": (None, [vp]),
         "rad_adapt_create": (C.c_int, [vp, vp, P(Options), i32, P(vp)]),
+        "rad_adapt_device_stats": (C.c_int, [vp, P(i64), P(i64), P(i64)]),
         "rad_adapt_run": (C.c_int, [vp, i64, P(i64), P(i32)]),
         "rad_adapt_trace": (C.c_int, [vp, vp, i64, P(i64)]),
         "rad_adapt_stats": (C.c_int, [vp, P(Stats), P(i64), P(i64), P(i64)]),
@@ -411,6 +415,7 @@ class Batch:
     def __init__(self, scenes, trees, opts, device: int = 0, trace_cap: int = 0):
         n = len(scenes)
         self._keep = (list(scenes), list(trees), list(opts))
+        self.P = max(1, int(opts[0].parallel_src)) if n else 1
         sp = (C.c_void_p * n)(*[s.h.value for s in scenes])
         tp = (C.c_void_p * n)(*[t.h.value for t in trees])
         op = (Options * n)(*opts)
@@ -445,7 +450,7 @@ class Batch:
         out = np.zeros(n.value, np.int32)
         if n.value:
             _check(load().rad_batch_trace(self.h, s, out.ctypes.data, n.value, C.byref(n)))
-        return out.reshape(-1, 1)
+        return out.reshape(-1, self.P)
 
     def stats(self) -> Dict[str, int]:
         s = Stats()
@@ -454,6 +459,18 @@ class Batch:
 
     def set_counting(self, on: bool):
         _check(load().rad_batch_set_counting(self.h, 1 if on else 0))
+
+    @property
+    def form(self) -> int:
+        return int(load().rad_batch_form(self.h))
+
+    def set_form(self, form: int):
+        _check(load().rad_batch_set_form(self.h, form))
+
+    def autotune(self, iters_per_trial: int = 4, rounds: int = 3) -> int:
+        ch = C.c_int32()
+        _check(load().rad_batch_autotune(self.h, iters_per_trial, rounds, C.byref(ch)))
+        return ch.value
 
     def close(self):
         if self.h:
@@ -494,6 +511,9 @@ class Adaptive:
         _check(load().rad_adapt_stats(self.h, C.byref(s), C.byref(hp), C.byref(sp), C.byref(sm)))
         d = {k: getattr(s, k) for k, _ in Stats._fields_}
         d.update(host_points=hp.value, splits=sp.value, samples=sm.value)
+        dp, sl, sc = C.c_int64(), C.c_int64(), C.c_int64()
+        _check(load().rad_adapt_device_stats(self.h, C.byref(dp), C.byref(sl), C.byref(sc)))
+        d.update(device_points=dp.value, speculations=sl.value, split_candidates=sc.value)
         return d
 
     def close(self):

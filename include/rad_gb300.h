@@ -102,6 +102,7 @@ typedef struct rad_stats {
     double unshot_power;    /* sum over live slots of (dB_r + dB_g + dB_b) * area, reduced in
                                FP64 in a fixed order: the convergence monitor (rad_dev_stats
                                only; selection keeps the reference's FP32 key, rad.cpp:394) */
+    int64_t h2d_bytes;      /* bytes copied host -> device when the handle was created */
 } rad_stats;
 
 void rad_options_default(rad_options* o);
@@ -229,12 +230,11 @@ int rad_dev_ray_hit(rad_dev* d, const void* p, const void* v, const int32_t* ban
  * rcv[i] from shooter slot src (AdaptCalFF(CalFF(...)), src/shade.cpp:442-450). */
 int rad_dev_form_factors(rad_dev* d, int32_t src, const int32_t* rcv, int32_t n, void* ff);
 /* Form factors without allocating: the variant of rad_dev_form_factors for
- * callers that must not call cudaMalloc or cudaFree at this point -- code
- * inside a CUDA graph capture it owns (an allocation would break the
- * capture), a render or simulation loop with a fixed device-memory budget
- * whose allocator owns all memory, or a real-time loop that cannot take an
- * allocation's synchronisation.  No counterpart in the reference (its
- * CalFF runs on host memory only).
+ * callers that cannot call cudaMalloc or cudaFree when they call this -- a
+ * renderer or simulation loop whose own allocator holds the whole device
+ * memory budget, or a real-time loop that cannot take the implicit
+ * synchronisation an allocation brings.  No counterpart in the reference
+ * (its CalFF runs on host memory only).
  *   src    host array of n_src shooter slots, 1 <= n_src <= 64
  *   d_rcv  device array of n_rcv receiver slots (caller-allocated)
  *   d_ff   device array of n_src * n_rcv * 3 reals (float, or double for a
@@ -248,9 +248,16 @@ int rad_dev_form_factors(rad_dev* d, int32_t src, const int32_t* rcv, int32_t n,
  * by every GPU that loads the library until exit) instead of allocated
  * memory; more than 64 shooters is RAD_ERR_CAPACITY.  Every call reuses that
  * array, so calls whose kernels can overlap on the GPU (different streams
- * without ordering) race on it; order them on one stream.  The first call on
- * each device looks the array's device address up (cudaGetSymbolAddress with
- * that device current): make that first call before any stream capture. */
+ * without ordering) race on it; order them on one stream.  The kernels also
+ * add to the handle's walk counters, so finish or order `stream` before any
+ * other call on the same handle.  The first call on each device looks the
+ * array's device address up (cudaGetSymbolAddress with that device current)
+ * and keeps it for the life of the process: make that first call before any
+ * stream capture, and do not call again after cudaDeviceReset.  The caller's
+ * current device is unchanged on return.  A walk stopped by walk_cap or by a
+ * repeated state gives form factor 0 for that corner, as an occluded ray
+ * does; such walks are counted only in the handle's rad_stats
+ * (walk_cap_hits, walk_loops), not per call. */
 int rad_dev_form_factors_noalloc(rad_dev* d, const int32_t* src, int32_t n_src, const int32_t* d_rcv, int32_t n_rcv,
                                  void* d_ff, void* stream);
 void rad_dev_destroy(rad_dev* d);
@@ -260,10 +267,15 @@ void rad_dev_destroy(rad_dev* d);
 /* Upload n_scenes independent scenes (each after init + pre-partition, with
  * its own options: converge limit, walk cap) for the batched form: every
  * iteration, each scene that has not converged does one shooter step of
- * parallelRadiosity (src/rad.cpp:406-451) with one shooter, all scenes in one
- * persistent launch.  FP32 only; parallel_src must be 1.  Each scene's result
- * is bit-identical to rad_dev_run on that scene.  trace_cap: shooter ids kept
- * per scene (default 65536 when <= 0). */
+ * parallelRadiosity (src/rad.cpp:406-451), all scenes in one persistent
+ * launch.  All scenes share one precision (32 or 64) and one -parallel_src P
+ * (listCanditate's top n per scene, src/rad.cpp:387-404).  FP32 with P = 1
+ * runs one kernel per iteration (the selection fused into its last CTA); FP64
+ * or P > 1 adds a selection kernel, one CTA per scene.  Each scene's result is
+ * bit-identical to rad_dev_run on that scene.  trace_cap: steps kept per
+ * scene in its trace (P entries each; default 65536 when <= 0).  The octree
+ * cells and list records are expanded on the device from the compact tables
+ * (a leaf per cell, a triangle per list entry). */
 int rad_batch_create(const rad_scene* const* scenes, const rad_octree* const* trees, const rad_options* opts,
                      int32_t n_scenes, int32_t trace_cap, int32_t device, rad_batch** out);
 /* Run up to max_iters batch iterations; stops when every scene converged.
@@ -279,6 +291,16 @@ int rad_batch_trace(const rad_batch* b, int32_t scene, int32_t* out, int64_t cap
 /* Totals over all scenes (steps = shooter steps of all scenes). */
 int rad_batch_stats(const rad_batch* b, rad_stats* st);
 int rad_batch_set_counting(rad_batch* b, int32_t on);
+/* The shooting kernel's form (no reference counterpart; results do not depend
+ * on it): 1 = 4 CTAs per SM (64 registers), 2 = 3 CTAs per SM (80 registers).
+ * FP32 batches start in form 1, FP64 in form 2. */
+int rad_batch_set_form(rad_batch* b, int32_t form);
+int rad_batch_form(const rad_batch* b);
+/* Choose the form by timing: one untimed iteration in each form, then
+ * `rounds` rounds of iters_per_trial (1..32) iterations in each form, in
+ * alternating order; the faster form per iteration is kept (*chosen).  The
+ * iterations are ordinary batch iterations (results unchanged). */
+int rad_batch_autotune(rad_batch* b, int32_t iters_per_trial, int32_t rounds, int32_t* chosen);
 void rad_batch_destroy(rad_batch* b);
 
 /* ---- adaptive split variant ---------------------------------------------- */
@@ -292,14 +314,24 @@ void rad_batch_destroy(rad_batch* b);
  * after rad_scene_init and WITHOUT rad_scene_prepartition (that configuration
  * has none).  The scene is updated in place by rad_adapt_run (topology,
  * accB, deltaB): write it with rad_scene_write_fin; it must outlive the
- * handle.  Each step's corner and centre form factors are computed on the
- * device; the receiver loop, splits and sample points run on the host. */
+ * handle.  Each step's corner and centre form factors, the delta-FF test of
+ * every receiver and the form factors of the sample points it draws are
+ * computed on the device (the sample points speculatively, at the rand()
+ * position they get if no earlier receiver breaks its sample loop); the
+ * receiver loop in slot order, the splits with their neighbour links and
+ * rollback, and every value whose inputs a split changed run on the host. */
 int rad_adapt_create(rad_scene* s, const rad_octree* t, const rad_options* o, int32_t device, rad_adapt** out);
 int rad_adapt_run(rad_adapt* a, int64_t max_steps, int64_t* steps_done, int32_t* converged);
 int rad_adapt_trace(const rad_adapt* a, int32_t* out, int64_t cap, int64_t* n);
 /* host_points: form factors evaluated on the host (sample points, receivers
  * rewritten earlier in their step); splits; rand() sample points drawn. */
 int rad_adapt_stats(const rad_adapt* a, rad_stats* st, int64_t* host_points, int64_t* splits, int64_t* samples);
+/* The device's share (no reference counterpart): sample points whose form
+ * factor came from the device's speculation, speculation launches, and
+ * receivers whose delta-FF test failed at the start of their step (summed
+ * over steps). */
+int rad_adapt_device_stats(const rad_adapt* a, int64_t* device_points, int64_t* speculations,
+                           int64_t* split_candidates);
 void rad_adapt_destroy(rad_adapt* a);
 
 /* ---------------------------------------------------------------- headless render

@@ -22,17 +22,32 @@ REF32 = os.path.join(HERE, "_ref", "rad_ref32")
 REF32C = os.path.join(HERE, "_ref", "rad_ref32c")
 REF64 = os.path.join(HERE, "_ref", "rad_ref64")
 REF32A = os.path.join(HERE, "_ref", "rad_ref32a")
+# the reference's own build flags (FP contraction on): timed, never compared
+REF_SHIPPED = os.path.join(HERE, "_ref", "rad_ref_shipped")
+REF_SHIPPED_FLAGS = "-O2 -fopenmp -std=c++11 -march=native (reference Makefile:7) + -include vector"
 
 
 def build_oracle() -> None:
     subprocess.run(["make", "-s", "-C", HERE, "oracle"], check=True)
 
 
+def reference_dir() -> Optional[str]:
+    """The reference tree (morris821028/hw-radiosity) to stage from, or None:
+    $RAD_REFERENCE_DIR, else baseline/_ref, else /root/reference -- the first
+    that holds a src/ directory.  On a machine without any of them the staged
+    copy under oracle/_ref is built as it is."""
+    repo = os.path.dirname(HERE)
+    for cand in (os.environ.get("RAD_REFERENCE_DIR"), os.path.join(repo, "baseline", "_ref"), "/root/reference"):
+        if cand and os.path.isdir(os.path.join(cand, "src")):
+            return cand
+    return None
+
+
 def build_ref(ref_root: Optional[str] = None) -> bool:
     """Stage (when the reference tree is present) and build the reference binaries.
     Returns True when oracle/_ref binaries exist afterwards."""
-    ref_root = ref_root or "/root/reference"
-    if os.path.isdir(os.path.join(ref_root, "src")):
+    ref_root = ref_root or reference_dir()
+    if ref_root and os.path.isdir(os.path.join(ref_root, "src")):
         subprocess.run(["python3", os.path.join(HERE, "stage_ref.py"), "--ref", ref_root], check=True,
                        capture_output=True)
     if os.path.isdir(os.path.join(HERE, "_ref", "src", "src")):

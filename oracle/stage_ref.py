@@ -138,9 +138,13 @@ def _to_fp64(files):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=None,
+                    help="reference tree (default: $RAD_REFERENCE_DIR, baseline/_ref, /root/reference)")
     ap.add_argument("--out", default=os.path.join(HERE, "_ref"))
     args = ap.parse_args()
+    if args.ref is None:
+        from runner import reference_dir
+        args.ref = reference_dir() or "(none found)"
     if not os.path.isdir(os.path.join(args.ref, "src")):
         print(f"stage_ref: no reference tree at {args.ref}; nothing staged", file=sys.stderr)
         return 1

@@ -30,7 +30,7 @@ from golden_cases import CASES, make_scene  # noqa: E402
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=None, help="reference tree (default: runner.reference_dir())")
     args = ap.parse_args()
     if not runner.build_ref(args.ref):
         sys.exit("reference binaries could not be built")

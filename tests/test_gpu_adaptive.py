@@ -1,8 +1,9 @@
 """Adaptive split variant (the reference built with ADAPT + ROLLBACK only):
-the device computes each step's corner and centre form factors, the host runs
-the receiver loop, splits and rand() sample points.  Results must equal the
-reference's adaptive build bit for bit: shooter sequence, split topology,
-per-vertex radiosity, .fin bytes."""
+the device computes each step's corner and centre form factors, the delta-FF
+test of every receiver and (speculatively) the form factors of its rand()
+sample points; the host runs the receiver loop and the splits.  Results must
+equal the reference's adaptive build bit for bit: shooter sequence, split
+topology, per-vertex radiosity, .fin bytes."""
 import hashlib
 import os
 import subprocess
@@ -50,6 +51,33 @@ def test_adaptive_matches_reference_fixture(built, workdir, name):
         assert hashlib.sha256(fh.read()).hexdigest() == idx["fin_sha256"]
     st = ad.stats()
     assert st["splits"] > 0 and st["rays"] > 0
+    if st["samples"]:
+        assert st["device_points"] > 0 and st["speculations"] > 0
+
+
+def test_adaptive_device_sample_points_bench_room(built, workdir):
+    """The bench's adaptive workload (100^3 room, 4 boxes, splitting toward
+    40,000 slots), 30 steps: equal to the oracle bit for bit, with most sample
+    points taken from the device's speculation."""
+    s = scenes.room_with_boxes(8, 4, 1, seed=5, size=100.0)
+    tri = s.write(os.path.join(workdir, "ad_bench.tri"))
+    argv = s.argv({"-triangle": "40000", "-converge": "5"})
+    o = capi.options_from_argv(argv)
+    sc = capi.Scene.load(tri, o)
+    tree = capi.Octree(sc, 4)
+    sc.init()
+    ad = capi.Adaptive(sc, tree, o)
+    for c in (1, 9, 20):
+        ad.run(c)
+    ref = runner.oracle(tri, argv, steps=30, adaptive=True)
+    assert np.array_equal(ad.trace(), runner.trace_array(ref["trace"]))
+    v = sc.view()
+    for k in ("parent", "p", "accB", "deltaB", "nb"):
+        assert same_bits(v[k], ref["dump"][k]), k
+    st = ad.stats()
+    assert st["samples"] > 1000
+    assert st["device_points"] > 0.7 * st["samples"]
+    assert st["host_points"] < 0.5 * st["samples"]
 
 
 def test_adaptive_fp64_equals_oracle(built, workdir):

@@ -89,3 +89,28 @@ def test_cli_host_preparation(built, workdir, flags):
     assert r.returncode == 0, r.stderr
     with open(prefix + ".fin", "rb") as fh:
         assert hashlib.sha256(fh.read()).hexdigest() == idx["fin_sha256"]
+
+
+def test_preparation_on_many_host_threads(built):
+    """Octrees and neighbour links of 24 batch rooms built on the device from
+    8 host threads at once (each thread with its own stream and device
+    scratch, kept between its calls) equal the host builds."""
+    from concurrent.futures import ThreadPoolExecutor
+    gens = scenes.batch_rooms(24, seed=61, lo=500, hi=8000)
+
+    def dev(g):
+        o = capi.options_from_argv(g.argv())
+        sc = capi.Scene.from_arrays(g.vtx, g.frgb, g.brgb, o)
+        t = capi.Octree(sc, device=0)
+        sc.init(device=0)
+        return sc, t
+
+    with ThreadPoolExecutor(8) as ex:
+        got = list(ex.map(dev, gens))
+    for g, (sc, t) in zip(gens, got):
+        o = capi.options_from_argv(g.argv())
+        sh = capi.Scene.from_arrays(g.vtx, g.frgb, g.brgb, o)
+        th = capi.Octree(sh, 2)
+        sh.init()
+        _assert_same_tree(t, th)
+        assert same_bits(sc.view()["nb"], sh.view()["nb"])

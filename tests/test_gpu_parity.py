@@ -241,31 +241,6 @@ def test_fp32_form_error_against_fp64_oracle(built, workdir):
     assert e_gpu == pytest.approx(e_ref, rel=0, abs=0)   # identical, as the FP32 solver equals the FP32 build
 
 
-def test_hall_bounded_steps_equal_oracle(built, workdir):
-    """The 40x20x100 hall: 406,684 triangles plus 300 pillars, pre-partitioned
-    to 422,429 slots; about 2.5M walks per step with ~140 triangle tests each."""
-    s = scenes.hall()
-    tri = s.write(os.path.join(workdir, "hall.tri"))
-    argv = s.argv()
-    steps = 2
-    o = capi.options_from_argv(argv)
-    sc = capi.Scene.load(tri, o)
-    tree = capi.Octree(sc, 8)
-    sc.init()
-    sc.prepartition()
-    dv = capi.Device(sc, tree, o)
-    assert dv.layout == 2   # over 4 groups per resident warp: the throughput form
-    n, conv, _ = dv.run(steps)
-    assert n == steps
-    dv.download(sc)
-    ref = runner.oracle(tri, argv, steps=steps, timeout=900)
-    assert np.array_equal(dv.trace(), runner.trace_array(ref["trace"]))
-    v = sc.view()
-    assert v["n"] == ref["dump"]["n"] == 422429
-    for k in ("accB", "deltaB"):
-        assert same_bits(v[k], ref["dump"][k]), k
-
-
 @pytest.mark.parametrize("fp64", [False, True])
 def test_unshot_power_monitor(built, workdir, fp64):
     """rad_stats.unshot_power: the FP64 total of (dB_r + dB_g + dB_b) * area over

@@ -23,9 +23,10 @@ def _scene_cases(workdir):
     c.append(("boxes", s.write(os.path.join(workdir, "h_boxes.tri")), s.argv({"-triangle": "4000"})))
     s = scenes.room(3, size=40.0, emitter=(0.3, 0.7))
     c.append(("coarse", s.write(os.path.join(workdir, "h_coarse.tri")), s.argv({"-triangle": "900"})))
-    if os.path.isdir("/root/reference/model"):
+    ref = runner.reference_dir()
+    if ref and os.path.isdir(os.path.join(ref, "model")):
         for m in ("box", "model2s", "room", "blocks", "church"):
-            c.append((m, f"/root/reference/model/{m}.tri", ["-triangle", "3000"]))
+            c.append((m, os.path.join(ref, "model", f"{m}.tri"), ["-triangle", "3000"]))
     return c
 
 

@@ -10,7 +10,7 @@ import runner
 from helpers import EDGE_SCENES, same_bits, write_edge_scene
 from hwrad import scenes
 
-REF_MODELS = "/root/reference/model"
+REF_MODELS = os.path.join(runner.reference_dir() or "", "model")
 
 
 def _cases(workdir):

@@ -50,3 +50,51 @@ def test_single_rank_has_no_collective():
     import bench
     r = bench.Ranks(1, "gloo")
     assert r.dist is None and r.max(3.5) == 3.5
+
+
+def _shard_worker(rank, world, port, out):
+    """Each rank takes its share of the 256-room batch (balanced by triangle
+    count, no data exchanged); the shares are gathered only to check them."""
+    import sys
+    sys.path.insert(0, REPO)
+    sys.path.insert(0, os.path.join(REPO, "hw-radiosity_gb300"))
+    os.environ.update({"MASTER_ADDR": "127.0.0.1", "MASTER_PORT": str(port), "RANK": str(rank),
+                       "WORLD_SIZE": str(world), "LOCAL_RANK": str(rank)})
+    import torch.distributed as dist
+    from hwrad import scenes, shard
+    import bench
+    w, r, _ = bench.rank_env()
+    ranks = bench.Ranks(w, "gloo")
+    tris = [len(g.vtx) for g in scenes.batch_rooms(256, seed=4000)]
+    mine = shard.partition_scenes(tris, w)[r]
+    shares = [None] * w
+    dist.all_gather_object(shares, mine)
+    total = ranks.sum(float(sum(tris[i] for i in mine)))
+    out[r] = (shares, total, sum(tris[i] for i in mine))
+    ranks.barrier()
+    ranks.close()
+
+
+def test_batch_scene_shards_cover_every_scene_once_gloo():
+    world = 2
+    mgr = mp.Manager()
+    out = mgr.dict()
+    mp.spawn(_shard_worker, args=(world, _free_port(), out), nprocs=world, join=True)
+    shares0, total0, load0 = out[0]
+    shares1, total1, load1 = out[1]
+    assert shares0 == shares1                       # every rank computed the same partition
+    flat = sorted(i for s in shares0 for i in s)
+    assert flat == list(range(256))                 # each scene exactly once
+    assert total0 == total1 == load0 + load1        # the sum over ranks is the whole batch
+    assert max(load0, load1) / min(load0, load1) < 1.01   # balanced by triangle count
+
+
+def test_partition_scenes_edges():
+    import sys
+    sys.path.insert(0, os.path.join(REPO, "hw-radiosity_gb300"))
+    from hwrad import shard
+    assert shard.partition_scenes([], 3) == [[], [], []]
+    assert shard.partition_scenes([5, 1, 1], 1) == [[0, 1, 2]]
+    assert shard.partition_scenes([5, 1, 1, 1], 2) == [[0], [1, 2, 3]]
+    parts = shard.partition_scenes([3, 3, 3], 5)
+    assert sorted(i for p in parts for i in p) == [0, 1, 2] and sum(1 for p in parts if not p) == 2

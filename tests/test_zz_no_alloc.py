@@ -1,6 +1,7 @@
-"""rad_dev_form_factors_noalloc: the form-factor query for callers that may
-not allocate device memory at the call (inside their own graph capture, under
-a fixed memory budget, or in a real-time loop).
+"""rad_dev_form_factors_noalloc: the form-factor query for callers that
+cannot allocate device memory at the call (a renderer or simulation loop whose
+own allocator holds the memory budget, or a real-time loop that cannot take
+an allocation's synchronisation).
 
 The caller owns the receiver and output buffers (here: torch tensors); the
 entry point keeps its shooter records in a fixed device array.  Its results
@@ -42,8 +43,10 @@ def test_noalloc_equals_allocating_entry_point(built, workdir, fp64):
     calls = [rng.choice(n, 7, replace=False).astype(np.int32), rng.choice(n, 64, replace=False).astype(np.int32)]
     for src in calls:   # two calls in a row: the second reuses the first's scratch
         d_ff = torch.full((len(src), len(rcv), 3), float("nan"), dtype=tt, device="cuda")
+        dev_before = torch.cuda.current_device()
         rc = dv.form_factors_noalloc(src, d_rcv.data_ptr(), len(rcv), d_ff.data_ptr(), stream)
         assert rc == capi.RAD_OK, capi.load().rad_last_error()
+        assert torch.cuda.current_device() == dev_before   # the caller's current device is left as it was
         torch.cuda.synchronize()
         got = d_ff.cpu().numpy()
         for s_i, s in enumerate(src):
