@@ -193,6 +193,33 @@ static V lights(const U& u, V n, V e, const V* ld) {
     return w;
 }
 
+/* The viewer's vertex stage (flat.vs, gouraud.vs): eye-space position MV x v,
+ * normal N x n, direction to light i normalize(L_i - position). */
+static V eye_pos(const U& u, float x, float y, float z) {
+    const float* M = u.MV;
+    return mk(M[0] * x + M[4] * y + M[8] * z + M[12], M[1] * x + M[5] * y + M[9] * z + M[13],
+              M[2] * x + M[6] * y + M[10] * z + M[14]);
+}
+static V eye_nrm(const U& u, float a, float b, float c) {
+    const float* N = u.N;
+    return mk(N[0] * a + N[3] * b + N[6] * c, N[1] * a + N[4] * b + N[7] * c, N[2] * a + N[5] * b + N[8] * c);
+}
+static V light_dir(const U& u, int i, V vp) { return nz(sb(mk(u.L[i][0], u.L[i][1], u.L[i][2]), vp)); }
+/* gouraud.vs's colour of a vertex (eye position vp, eye normal vn, colour cc) */
+static V gouraud_colour(const U& u, V vp, V vn, V cc) {
+    V ld[3];
+    for (int i = 0; i < 3; i++) ld[i] = light_dir(u, i, vp);
+    const V w = lights(u, nz(vn), nz(mk(-vp.x, -vp.y, -vp.z)), ld);
+    return mk(cc.x * w.x, cc.y * w.y, cc.z * w.z);
+}
+/* flat.fs's colour of a fragment: face normal tn, interpolated varyings a
+ * (eye position 0-2, light directions 3-11, colour 12-14) */
+static V flat_colour(const U& u, V tn, const float* a) {
+    const V ld[3] = {mk(a[3], a[4], a[5]), mk(a[6], a[7], a[8]), mk(a[9], a[10], a[11])};
+    const V w = lights(u, tn, nz(mk(-a[0], -a[1], -a[2])), ld);
+    return mk(a[12] * w.x, a[13] * w.y, a[14] * w.z);
+}
+
 static bool tl(float ax, float ay, float bx, float by) { return (ay == by && bx < ax) || (by < ay); }
 
 static unsigned char b8(float c) {
@@ -213,18 +240,14 @@ static void render(const std::vector<float>& Pp, const std::vector<float>& Nn, c
         float cx[3], cy[3], cz[3], cw[3];
         for (int k = 0; k < 3; k++) {
             const float x = Pp[t * 9 + k * 3], y = Pp[t * 9 + k * 3 + 1], z = Pp[t * 9 + k * 3 + 2];
-            const float* M = u.MV;
-            r.vp[k] = mk(M[0] * x + M[4] * y + M[8] * z + M[12], M[1] * x + M[5] * y + M[9] * z + M[13],
-                         M[2] * x + M[6] * y + M[10] * z + M[14]);
+            r.vp[k] = eye_pos(u, x, y, z);
             const float* P = u.P;
             const V q = r.vp[k];
             cx[k] = P[0] * q.x + P[4] * q.y + P[8] * q.z + P[12];
             cy[k] = P[1] * q.x + P[5] * q.y + P[9] * q.z + P[13];
             cz[k] = P[2] * q.x + P[6] * q.y + P[10] * q.z + P[14];
             cw[k] = P[3] * q.x + P[7] * q.y + P[11] * q.z + P[15];
-            const float a = Nn[t * 9 + k * 3], b = Nn[t * 9 + k * 3 + 1], c = Nn[t * 9 + k * 3 + 2];
-            const float* N = u.N;
-            r.vn[k] = mk(N[0] * a + N[3] * b + N[6] * c, N[1] * a + N[4] * b + N[7] * c, N[2] * a + N[5] * b + N[8] * c);
+            r.vn[k] = eye_nrm(u, Nn[t * 9 + k * 3], Nn[t * 9 + k * 3 + 1], Nn[t * 9 + k * 3 + 2]);
             if (!(cw[k] > 0.f)) r.ok = 0;
         }
         r.ord[0] = 0; r.ord[1] = 1; r.ord[2] = 2;
@@ -284,14 +307,15 @@ static void render(const std::vector<float>& Pp, const std::vector<float>& Nn, c
             for (int k = 0; k < 3; k++) {
                 const int s = r.ord[k];
                 const V cc = mk(Cc[t * 9 + s * 3], Cc[t * 9 + s * 3 + 1], Cc[t * 9 + s * 3 + 2]);
-                V ld[3];
-                for (int i = 0; i < 3; i++) ld[i] = nz(sb(mk(u.L[i][0], u.L[i][1], u.L[i][2]), r.vp[s]));
                 if (u.shading == 1) {
-                    const V w = lights(u, nz(r.vn[s]), nz(mk(-r.vp[s].x, -r.vp[s].y, -r.vp[s].z)), ld);
-                    vary[k][0] = cc.x * w.x; vary[k][1] = cc.y * w.y; vary[k][2] = cc.z * w.z;
+                    const V g = gouraud_colour(u, r.vp[s], r.vn[s], cc);
+                    vary[k][0] = g.x; vary[k][1] = g.y; vary[k][2] = g.z;
                 } else {
                     vary[k][0] = r.vp[s].x; vary[k][1] = r.vp[s].y; vary[k][2] = r.vp[s].z;
-                    for (int i = 0; i < 3; i++) { vary[k][3 + 3 * i] = ld[i].x; vary[k][4 + 3 * i] = ld[i].y; vary[k][5 + 3 * i] = ld[i].z; }
+                    for (int i = 0; i < 3; i++) {
+                        const V ld = light_dir(u, i, r.vp[s]);
+                        vary[k][3 + 3 * i] = ld.x; vary[k][4 + 3 * i] = ld.y; vary[k][5 + 3 * i] = ld.z;
+                    }
                     vary[k][12] = cc.x; vary[k][13] = cc.y; vary[k][14] = cc.z;
                 }
             }
@@ -303,9 +327,8 @@ static void render(const std::vector<float>& Pp, const std::vector<float>& Nn, c
                 c0 = a[0]; c1 = a[1]; c2 = a[2];
             } else {
                 const V tn = nz(cr(sb(r.vp[r.ord[1]], r.vp[r.ord[0]]), sb(r.vp[r.ord[2]], r.vp[r.ord[0]])));
-                const V ld[3] = {mk(a[3], a[4], a[5]), mk(a[6], a[7], a[8]), mk(a[9], a[10], a[11])};
-                const V w = lights(u, tn, nz(mk(-a[0], -a[1], -a[2])), ld);
-                c0 = a[12] * w.x; c1 = a[13] * w.y; c2 = a[14] * w.z;
+                const V c = flat_colour(u, tn, a);
+                c0 = c.x; c1 = c.y; c2 = c.z;
             }
             o[0] = b8(c0); o[1] = b8(c1); o[2] = b8(c2); o[3] = 255;
         }

@@ -171,6 +171,20 @@ def main():
             os.makedirs(os.path.dirname(p), exist_ok=True)
             with open(p, "w") as f:
                 f.write(text)
+    # the result viewer's shaders, made compilable as C++ against
+    # oracle/glsl_shim.h: the #extension and precision lines dropped and the
+    # swizzles .xyz .rgb .a .s .t written as calls; nothing else changes
+    lib = os.path.join(args.ref, "WebGL_demo", "public", "lib")
+    if os.path.isdir(lib):
+        out = os.path.join(args.out, "src_shaders")
+        os.makedirs(out, exist_ok=True)
+        for name in ("gouraud.vs", "flat.vs", "flat.fs"):
+            with open(os.path.join(lib, name)) as f:
+                lines = f.read().splitlines()
+            kept = [ln for ln in lines if not re.match(r"\s*(#extension|precision)\b", ln)]
+            text = re.sub(r"\.(xyz|rgb|a|s|t)\b", r".\1()", "\n".join(kept) + "\n")
+            with open(os.path.join(out, name), "w") as f:
+                f.write(text)
     # the result viewer's model converter (one file, unpatched): pins the
     # converter half of the headless renderer's input preparation
     conv = os.path.join(args.ref, "WebGL_demo", "model-converter", "main.cpp")

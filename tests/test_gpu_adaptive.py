@@ -51,8 +51,6 @@ def test_adaptive_matches_reference_fixture(built, workdir, name):
         assert hashlib.sha256(fh.read()).hexdigest() == idx["fin_sha256"]
     st = ad.stats()
     assert st["splits"] > 0 and st["rays"] > 0
-    if st["samples"]:
-        assert st["device_points"] > 0 and st["speculations"] > 0
 
 
 def test_adaptive_device_sample_points_bench_room(built, workdir):

@@ -68,3 +68,27 @@ def test_render_argument_errors(built, workdir):
     s = capi.render_options(width=2, height=2)
     s.shading = 7
     assert L.rad_render_fin(bad.encode(), s, 0, img.ctypes.data) == capi.RAD_ERR_ARG
+
+
+SHADER_PIN = os.path.join(runner.HERE, "_ref", "shader_pin")
+
+
+@pytest.mark.skipif(not os.path.isdir(os.path.join(runner.HERE, "_ref", "src_shaders")),
+                    reason="the viewer's shader sources were not staged (no reference tree)")
+def test_viewer_shader_sources_equal_the_restatement(built):
+    """The shader half: the viewer's own gouraud.vs, flat.vs and flat.fs,
+    compiled as C++ against oracle/glsl_shim.h (builtins as the shim states
+    them), against the restatement's vertex and fragment stages that its
+    render() and the CUDA rasteriser follow -- bit for bit on 600k seeded
+    vertices and fragments in three views.  Clip positions are only reported
+    (the shader multiplies P x MV first); they must agree to a small fraction
+    of a pixel."""
+    import subprocess as sp
+    sp.run(["make", "-s", "-C", runner.HERE, "_ref/shader_pin"], check=True)
+    r = sp.run([SHADER_PIN, "200000"], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    w = r.stdout.split()
+    vals = {w[i]: w[i + 1] for i in range(0, len(w) - 1, 2)}
+    assert int(vals["samples"]) == 600000
+    assert vals["gouraud_vs_mismatch"] == vals["flat_vs_mismatch"] == vals["flat_fs_mismatch"] == "0"
+    assert float(vals["gl_position_max_window_diff_px"]) < 0.01
