@@ -29,6 +29,7 @@
 // T = double it is the all-FP64 form.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -60,14 +61,20 @@ constexpr double kHeavyMeanMult = 2.5;
 // group time starts early in the next step
 constexpr double kEarlyMeanMult = 1.5;
 // Two forms of the single-shooter kernel, picked per scene (layout):
-//   1 (tail-bound: a step is about one wave of groups) -- 3 CTAs per SM, 80
-//     registers, a split group's items cast each corner with 4 lanes that
-//     share the list scans, so a long walk ends sooner;
+//   1 (tail-bound: a step is about one wave of groups) -- a split group's
+//     items cast each corner with 4 lanes that share the list scans, so a
+//     long walk ends sooner; 4 CTAs per SM (64 registers) in FP32, 3 (80) in
+//     FP64, which spills far more at 64;
 //   2 (throughput-bound: many groups per warp, e.g. 400k triangles) -- 4 CTAs
 //     per SM, 64 registers, split items keep one lane per corner (3 slots
-//     per item) so the walk is inlined once and more warps hide latency.
-// Measured: the 61k-triangle room 9.4k vs 7.7k shots/s (flushed) in form 1
-// vs 2; the 422k-triangle hall 813 vs 997 shots/s.
+//     per item) so the walk is inlined once.
+// Measured: the 61k-triangle room 10.1k vs 8.2k shots/s (flushed) in form 1
+// vs 2; the 422k-triangle hall 794 vs 1,087 shots/s.  Form 1 at 3 CTAs per SM
+// (80 registers) measured 9.5k on the room.
+// The counting kernels and the several-shooters kernel (which cannot re-read
+// the deposit inputs after the walk) stay at 3 CTAs per SM.
+template <typename T>
+constexpr int kForm1MinBlocks = std::is_same<T, float>::value ? 4 : 3;
 template <int HL>
 __host__ __device__ constexpr int heavy_slots() { return HL == 1 ? 3 : 32 / (3 * HL); }
 template <int HL>
@@ -138,16 +145,18 @@ k_shoot(Slots<T> S, Grid<T> G, Shooter<T>* shooters, State* st, Partial* __restr
         }
         // one call site when every item is cast one lane per corner: the
         // walk is inlined once, which keeps the register count down
-        // FUSED: at most one shooter per step.  One-lane items then re-read
-        // the deposit's inputs after the walk instead of holding them in
-        // registers (ONE); measured 3-4% faster in form 2 and in the batched
-        // kernel, while the 4-lane items of form 1 measured 20-25% slower
-        // that way, so they keep the registers.
+        // FUSED: at most one shooter per step.  Items then re-read the
+        // deposit's inputs after the walk instead of holding them in
+        // registers (ONE): 3-4% faster in form 2 and in the batched kernel,
+        // and what lets form 1 run 4 CTAs per SM (6% faster on the 61k room
+        // than 3 CTAs per SM without it).  At 3 CTAs per SM (FP64) the 4-lane
+        // items keep their registers: 20-25% slower otherwise.
+        constexpr bool kOneHeavy = FUSED && MINB >= 4;
         if constexpr (HL == 1 || COUNT) {
             shoot_item<T, COUNT, 1, FUSED>(S, Gs, sh, nsh, i0, n_item, lane, conv, kk, ks, c);
         } else {
             if (g < n_heavy_items)
-                shoot_item<T, false, HL, false>(S, Gs, sh, nsh, i0, n_item, lane, conv, kk, ks, c);
+                shoot_item<T, false, HL, kOneHeavy>(S, Gs, sh, nsh, i0, n_item, lane, conv, kk, ks, c);
             else
                 shoot_item<T, COUNT, 1, FUSED>(S, Gs, sh, nsh, i0, n_item, lane, conv, kk, ks, c);
         }
@@ -446,6 +455,7 @@ struct DevImpl : DevBase {
     long long trace_cap = 0;
     int n_cta = 0;          // CTAs of the current layout's kernel
     int n_cta1 = 0, n_cta2 = 0;
+    int n_cta_nf = 0;       // the counting kernels and the several-shooters kernel (3 CTAs per SM)
     int n_cta_of(int l) const { return l == 2 ? n_cta2 : n_cta1; }
     int layout = 1;         // 1 tail-bound form, 2 throughput form (FP32, one shooter per step)
     int P = 1;
@@ -559,7 +569,7 @@ int upload(const Scene<T>& s, const Octree<T>& o, const rad_options& opt, int de
     if (d.shoot_smem() > 48 * 1024) {
         CU(cudaFuncSetAttribute(k_shoot<T, false, false, 3, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)d.shoot_smem()));
         CU(cudaFuncSetAttribute(k_shoot<T, true, false, 3, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)d.shoot_smem()));
-        CU(cudaFuncSetAttribute(k_shoot<T, false, true, 3, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)d.shoot_smem()));
+        CU(cudaFuncSetAttribute(k_shoot<T, false, true, kForm1MinBlocks<T>, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)d.shoot_smem()));
         CU(cudaFuncSetAttribute(k_shoot<T, true, true, 3, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)d.shoot_smem()));
         if constexpr (std::is_same<T, float>::value)
             CU(cudaFuncSetAttribute(k_shoot<T, false, true, 4, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -569,7 +579,9 @@ int upload(const Scene<T>& s, const Octree<T>& o, const rad_options& opt, int de
     {
         int sms = 0, per1 = 0, per2 = 0;
         CU(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
-        CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per1, k_shoot<T, false, true, 3, 4>, kShootThreads, d.shoot_smem()));
+        CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per1, k_shoot<T, false, true, kForm1MinBlocks<T>, 4>, kShootThreads, d.shoot_smem()));
+        int per_nf = 0;
+        CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_nf, k_shoot<T, false, false, 3, 4>, kShootThreads, d.shoot_smem()));
         if constexpr (std::is_same<T, float>::value)
             CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per2, k_shoot<T, false, true, 4, 1>, kShootThreads,
                                                              d.shoot_smem()));
@@ -577,6 +589,7 @@ int upload(const Scene<T>& s, const Octree<T>& o, const rad_options& opt, int de
             per2 = per1;
         const int want = (n_groups + kShootThreads / 32 - 1) / (kShootThreads / 32);
         d.n_cta1 = std::max(1, std::min(want, std::max(1, sms * per1)));
+        d.n_cta_nf = std::max(1, std::min(want, std::max(1, sms * per_nf)));
         d.n_cta2 = std::max(1, std::min(want, std::max(1, sms * per2)));
         // the throughput form once there are over 4 groups per resident warp
         const long long warps2 = (long long)sms * std::max(per2, 1) * (kShootThreads / 32);
@@ -585,7 +598,7 @@ int upload(const Scene<T>& s, const Octree<T>& o, const rad_options& opt, int de
     }
     int *d_heavy, *d_stamp, *d_early, *d_estamp;
     if ((rc = d.alloc(&d.d_shooters, (size_t)d.P)) || (rc = d.alloc(&d.d_state, 1)) ||
-        (rc = d.alloc(&d.d_part, (size_t)std::max(d.n_cta1, d.n_cta2))) || (rc = d.alloc(&d_heavy, 2 * (size_t)n_groups)) ||
+        (rc = d.alloc(&d.d_part, (size_t)std::max({d.n_cta1, d.n_cta2, d.n_cta_nf}))) || (rc = d.alloc(&d_heavy, 2 * (size_t)n_groups)) ||
         (rc = d.alloc(&d_stamp, (size_t)n_groups)) || (rc = d.alloc(&d.d_unshot, (size_t)kUnshotCtas + 1)) ||
         (rc = d.alloc(&d_early, 2 * (size_t)n_groups)) || (rc = d.alloc(&d_estamp, (size_t)n_groups)))
         return rc;
@@ -613,7 +626,7 @@ int upload(const Scene<T>& s, const Octree<T>& o, const rad_options& opt, int de
     CU(cudaMemcpyAsync(d.d_state, &st, sizeof st, cudaMemcpyHostToDevice, d.stream));
     d.h2d_bytes += (long long)sizeof st;
     CU(cudaMemsetAsync(d.d_shooters, 0, sizeof(Shooter<T>) * d.P, d.stream));
-    CU(cudaMemsetAsync(d.d_part, 0, sizeof(Partial) * std::max(d.n_cta1, d.n_cta2), d.stream));
+    CU(cudaMemsetAsync(d.d_part, 0, sizeof(Partial) * std::max({d.n_cta1, d.n_cta2, d.n_cta_nf}), d.stream));
     // initial selection keys: a step with no shooter only reduces the keys
     launch_shoot(d, d.stream);
     CU(cudaGetLastError());
@@ -628,24 +641,25 @@ int upload(const Scene<T>& s, const Octree<T>& o, const rad_options& opt, int de
 template <typename T>
 void launch_shoot(DevImpl<T>& d, cudaStream_t s) {
     const bool fused = d.P == 1;
-    // counting, several shooters per step and FP64 use the tail-bound form
+    // counting and several shooters per step use the tail-bound form at 3
+    // CTAs per SM (they cannot re-read the deposit inputs); FP64 uses form 1
     if (d.counting && fused)
-        k_shoot<T, true, true, 3, 4><<<d.n_cta1, kShootThreads, d.shoot_smem(), s>>>(d.S, d.G, d.d_shooters, d.d_state, d.d_part, d.conv);
+        k_shoot<T, true, true, 3, 4><<<d.n_cta_nf, kShootThreads, d.shoot_smem(), s>>>(d.S, d.G, d.d_shooters, d.d_state, d.d_part, d.conv);
     else if (d.counting)
-        k_shoot<T, true, false, 3, 4><<<d.n_cta1, kShootThreads, d.shoot_smem(), s>>>(d.S, d.G, d.d_shooters, d.d_state, d.d_part, d.conv);
+        k_shoot<T, true, false, 3, 4><<<d.n_cta_nf, kShootThreads, d.shoot_smem(), s>>>(d.S, d.G, d.d_shooters, d.d_state, d.d_part, d.conv);
     else if (fused && d.layout == 2) {
         if constexpr (std::is_same<T, float>::value)
             k_shoot<T, false, true, 4, 1><<<d.n_cta2, kShootThreads, d.shoot_smem(), s>>>(d.S, d.G, d.d_shooters, d.d_state,
                                                                                        d.d_part, d.conv);
     } else if (fused)
-        k_shoot<T, false, true, 3, 4><<<d.n_cta1, kShootThreads, d.shoot_smem(), s>>>(d.S, d.G, d.d_shooters, d.d_state, d.d_part, d.conv);
+        k_shoot<T, false, true, kForm1MinBlocks<T>, 4><<<d.n_cta1, kShootThreads, d.shoot_smem(), s>>>(d.S, d.G, d.d_shooters, d.d_state, d.d_part, d.conv);
     else
-        k_shoot<T, false, false, 3, 4><<<d.n_cta1, kShootThreads, d.shoot_smem(), s>>>(d.S, d.G, d.d_shooters, d.d_state, d.d_part, d.conv);
+        k_shoot<T, false, false, 3, 4><<<d.n_cta_nf, kShootThreads, d.shoot_smem(), s>>>(d.S, d.G, d.d_shooters, d.d_state, d.d_part, d.conv);
 }
 
 template <typename T>
 int launch_step(DevImpl<T>& d, cudaStream_t s) {
-    if (d.P > 1) k_setup<T><<<1, kSetupThreads, 0, s>>>(d.S, d.d_shooters, d.d_state, d.d_part, d.n_cta1, d.conv, d.P);
+    if (d.P > 1) k_setup<T><<<1, kSetupThreads, 0, s>>>(d.S, d.d_shooters, d.d_state, d.d_part, d.n_cta_nf, d.conv, d.P);
     launch_shoot(d, s);
     CU(cudaGetLastError());
     return RAD_OK;
@@ -718,7 +732,7 @@ int run(DevImpl<T>& d, long long max_steps, long long* done_steps, int* converge
         if (mode == 2) {
             // one step per iteration, kernels timed separately
             CU(cudaEventRecord(d.ev[0], d.stream));
-            if (d.P > 1) k_setup<T><<<1, kSetupThreads, 0, d.stream>>>(d.S, d.d_shooters, d.d_state, d.d_part, d.n_cta1, d.conv, d.P);
+            if (d.P > 1) k_setup<T><<<1, kSetupThreads, 0, d.stream>>>(d.S, d.d_shooters, d.d_state, d.d_part, d.n_cta_nf, d.conv, d.P);
             CU(cudaEventRecord(d.ev[1], d.stream));
             launch_shoot(d, d.stream);
             CU(cudaGetLastError());
