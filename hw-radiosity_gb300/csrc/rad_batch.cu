@@ -313,11 +313,17 @@ int graph_for(BatchImpl<T>& b, int iters, cudaGraphExec_t* out) {
     return RAD_OK;
 }
 
-// queue of (scene, group) items over the scenes still running
+// queue of (scene, group) items over the scenes still running, the scenes
+// with the most groups first: an iteration ends with its last item, and the
+// small scenes' short items fill the end (119.5k against 118.0k shots/s on
+// the 256-room batch in scene order).  Results do not depend on the order.
 template <typename T>
 int rebuild_items(BatchImpl<T>& b) {
     std::vector<int2> items;
-    for (int s = 0; s < b.n_scenes; s++) {
+    std::vector<int> ord(b.n_scenes);
+    for (int s = 0; s < b.n_scenes; s++) ord[s] = s;
+    std::stable_sort(ord.begin(), ord.end(), [&](int x, int y) { return b.desc[x].n_groups > b.desc[y].n_groups; });
+    for (int s : ord) {
         if (b.done[s]) continue;
         for (int g = 0; g < b.desc[s].n_groups; g++) items.push_back(make_int2(s, g));
     }
