@@ -67,6 +67,42 @@ private:
     std::vector<Buf> bufs_;
 };
 
+// Pinned host staging for uploads and downloads, per host thread, grow-only
+// and kept between calls.  The records a handle uploads are packed into it
+// and copied from it: packing into fresh pageable vectors paid a page fault
+// per 4 KB, and copying straight from the scene's pageable memory made the
+// host's next writes to those pages fault instead.  A call finishes its copies
+// before it returns, so the next call on the thread may reuse the buffer.
+class PinnedStage {
+public:
+    ~PinnedStage() {
+        int cur = 0;
+        if (p_ && cudaGetDevice(&cur) == cudaSuccess) cudaFreeHost(p_);
+    }
+    cudaError_t get(std::size_t bytes, void** out) {
+        if (bytes > cap_) {
+            if (p_) cudaFreeHost(p_);
+            p_ = nullptr;
+            cap_ = 0;
+            const std::size_t cap = bytes > 2 * cap_ ? bytes : 2 * cap_;
+            cudaError_t e = cudaHostAlloc(&p_, cap, cudaHostAllocPortable);
+            if (e != cudaSuccess) return e;
+            cap_ = cap;
+        }
+        *out = p_;
+        return cudaSuccess;
+    }
+
+private:
+    void* p_ = nullptr;
+    std::size_t cap_ = 0;
+};
+
+inline PinnedStage& pinned_stage() {
+    thread_local PinnedStage stage;
+    return stage;
+}
+
 // this thread's workspace for `device` (the device must be current)
 inline PrepWorkspace& prep_workspace(int device) {
     thread_local std::vector<std::unique_ptr<PrepWorkspace>> per_device;

@@ -34,10 +34,12 @@
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <thread>
 #include <type_traits>
 #include <vector>
 
 #include "capi_internal.h"
+#include "prep_workspace.h"
 
 #include "rad_kernels.cuh"
 
@@ -505,57 +507,105 @@ int upload(const Scene<T>& s, const Octree<T>& o, const rad_options& opt, int de
     const int n = s.trinum;
     if (n < 0) return fail(RAD_ERR_ARG, "negative slot count");
     if (!thresholds_consistent(o)) return fail(RAD_ERR_ARG, "octree cell thresholds do not match its dimensions");
-    // per-slot records, written in place (no per-element growth)
-    std::vector<Q4<T>> h_vtx((size_t)n * 3), h_acc((size_t)n * 3), h_nrm(n), h_ctr(n), h_frgb(n), h_db(n);
-    for (int i = 0; i < n; i++) {
-        const Slot<T>& t = s.slots[i];
-        for (int v = 0; v < 3; v++) {
-            h_vtx[(size_t)i * 3 + v] = {t.p[v][0], t.p[v][1], t.p[v][2], 0};
-            h_acc[(size_t)i * 3 + v] = {t.accB[v][0], t.accB[v][1], t.accB[v][2], 0};
-        }
-        const T nl = (T)std::sqrt(t.n[0] * t.n[0] + t.n[1] * t.n[1] + t.n[2] * t.n[2]);
-        h_nrm[i] = {t.n[0], t.n[1], t.n[2], nl};
-        h_ctr[i] = {t.c[0], t.c[1], t.c[2], t.area};
-        h_frgb[i] = {(T)t.Frgb[0], (T)t.Frgb[1], (T)t.Frgb[2], (T)t.parent};
-        h_db[i] = {t.deltaB[0], t.deltaB[1], t.deltaB[2], 0};
-    }
-    // the walk's triangle records, one group of five per triangle a list names
+    // The kernels' records are packed on the host into this thread's pinned
+    // staging (reused between handles, so no page faults) and copied from
+    // there: the six per-slot arrays as one block, then the walk's triangle
+    // records and the octree's compact tables, which are expanded on the
+    // device in this thread's preparation scratch.  Only the records the
+    // solver keeps are allocated for the handle.
     int n_tri = 0;
     for (int32_t id : o.entry_tri) n_tri = std::max(n_tri, id + 1);
     if (n_tri > n) return fail(RAD_ERR_ARG, "octree names a triangle beyond the scene");
-    std::vector<Q4<T>> h_trec((size_t)n_tri * 5);
-    for (int id = 0; id < n_tri; id++) {
-        const Slot<T>& t = s.slots[id];
-        Q4<T>* r = &h_trec[(size_t)id * 5];
-        r[0] = {t.n[0], t.n[1], t.n[2], pack_int<T>(id)};
-        r[1] = {t.c[0], t.c[1], t.c[2], 0};
-        for (int e = 0; e < 3; e++) r[2 + e] = {t.se[e][0], t.se[e][1], t.se[e][2], t.se[e][3]};
+    const long long n_cell = (long long)o.cell_leaf.size(), n_ent = (long long)o.entry_tri.size();
+    const size_t n_rec = (size_t)n * 10;            // vtx 3, acc 3, nrm, ctr, frgb, db per slot
+    const size_t n_trec = (size_t)n_tri * 5;
+    void* stage_p = nullptr;
+    CU(pinned_stage().get((n_rec + n_trec) * sizeof(Q4<T>), &stage_p));
+    Q4<T>* h_vtx = static_cast<Q4<T>*>(stage_p);
+    Q4<T>* h_acc = h_vtx + (size_t)n * 3;
+    Q4<T>* h_nrm = h_acc + (size_t)n * 3;
+    Q4<T>* h_ctr = h_nrm + n;
+    Q4<T>* h_frgb = h_ctr + n;
+    Q4<T>* h_db = h_frgb + n;
+    Q4<T>* h_trec = h_db + n;
+    // slots [a, b): their records, and the walk's triangle records of the
+    // triangles among them that a list names (five per triangle)
+    auto pack = [&](int a, int b) {
+        for (int i = a; i < b; i++) {
+            const Slot<T>& t = s.slots[i];
+            for (int v = 0; v < 3; v++) {
+                h_vtx[(size_t)i * 3 + v] = {t.p[v][0], t.p[v][1], t.p[v][2], 0};
+                h_acc[(size_t)i * 3 + v] = {t.accB[v][0], t.accB[v][1], t.accB[v][2], 0};
+            }
+            const T nl = (T)std::sqrt(t.n[0] * t.n[0] + t.n[1] * t.n[1] + t.n[2] * t.n[2]);
+            h_nrm[i] = {t.n[0], t.n[1], t.n[2], nl};
+            h_ctr[i] = {t.c[0], t.c[1], t.c[2], t.area};
+            h_frgb[i] = {(T)t.Frgb[0], (T)t.Frgb[1], (T)t.Frgb[2], (T)t.parent};
+            h_db[i] = {t.deltaB[0], t.deltaB[1], t.deltaB[2], 0};
+            if (i < n_tri) {
+                Q4<T>* r = &h_trec[(size_t)i * 5];
+                r[0] = {t.n[0], t.n[1], t.n[2], pack_int<T>(i)};
+                r[1] = {t.c[0], t.c[1], t.c[2], 0};
+                for (int e = 0; e < 3; e++) r[2 + e] = {t.se[e][0], t.se[e][1], t.se[e][2], t.se[e][3]};
+            }
+        }
+    };
+    // a memory-bound pass: large scenes split it over the -jobs host threads
+    const int jobs = n >= 16384 ? std::max(1, std::min({opt.jobs, 16, n / 8192})) : 1;
+    if (jobs <= 1) {
+        pack(0, n);
+    } else {
+        auto lo = [&](int j) { return (int)((long long)n * j / jobs); };
+        std::vector<std::thread> pool;
+        int started = 1;
+        try {
+            for (; started < jobs; started++) pool.emplace_back(pack, lo(started), lo(started + 1));
+        } catch (...) {   // chunks whose thread could not start are packed here
+        }
+        for (int j = started; j < jobs; j++) pack(lo(j), lo(j + 1));
+        pack(0, lo(1));
+        for (auto& th : pool) th.join();
     }
-    Q4<T> *d_vtx, *d_nrm, *d_ctr, *d_frgb, *d_acc, *d_db, *d_ent, *d_trec;
+    Q4<T>* d_rec;
+    Q4<T>* d_ent;
     CellRec<T>* d_cell;
-    T *d_thr, *d_lbox;
-    int32_t *d_cleaf, *d_lrange, *d_etri;
+    T* d_thr;
     int rc;
-    auto put = [&](auto** dst, const auto& src) -> int {
-        int r = d.alloc(dst, src.size());
-        if (r) return r;
-        CU(cudaMemcpyAsync(*dst, src.data(), src.size() * sizeof(src[0]), cudaMemcpyHostToDevice, d.stream));
-        d.h2d_bytes += (long long)(src.size() * sizeof(src[0]));
+    if ((rc = d.alloc(&d_rec, n_rec)) || (rc = d.alloc(&d_thr, o.thr.size())) || (rc = d.alloc(&d_cell, (size_t)n_cell)) ||
+        (rc = d.alloc(&d_ent, (size_t)n_ent * 5)))
+        return rc;
+    Q4<T>* d_vtx = d_rec;
+    Q4<T>* d_acc = d_vtx + (size_t)n * 3;
+    Q4<T>* d_nrm = d_acc + (size_t)n * 3;
+    Q4<T>* d_ctr = d_nrm + n;
+    Q4<T>* d_frgb = d_ctr + n;
+    Q4<T>* d_db = d_frgb + n;
+    auto h2d = [&](void* dst, const void* src, size_t bytes) -> int {
+        if (bytes) CU(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, d.stream));
+        d.h2d_bytes += (long long)bytes;
         return RAD_OK;
     };
-    const long long n_cell = (long long)o.cell_leaf.size(), n_ent = (long long)o.entry_tri.size();
-    if ((rc = put(&d_vtx, h_vtx)) || (rc = put(&d_nrm, h_nrm)) || (rc = put(&d_ctr, h_ctr)) ||
-        (rc = put(&d_frgb, h_frgb)) || (rc = put(&d_acc, h_acc)) || (rc = put(&d_db, h_db)) ||
-        (rc = put(&d_thr, o.thr)) || (rc = put(&d_cleaf, o.cell_leaf)) || (rc = put(&d_lbox, o.leaf_box)) ||
-        (rc = put(&d_lrange, o.leaf_range)) || (rc = put(&d_etri, o.entry_tri)) || (rc = put(&d_trec, h_trec)) ||
-        (rc = d.alloc(&d_cell, (size_t)n_cell)) || (rc = d.alloc(&d_ent, (size_t)n_ent * 5)))
+    PrepWorkspace& ws = prep_workspace(device);
+    void *t_trec, *t_cleaf, *t_lbox, *t_lrange, *t_etri;
+    CU(ws.buffer(8, std::max<size_t>(n_trec * sizeof(Q4<T>), 16), &t_trec));
+    CU(ws.buffer(9, std::max<size_t>(o.cell_leaf.size() * 4, 16), &t_cleaf));
+    CU(ws.buffer(10, std::max<size_t>(o.leaf_box.size() * sizeof(T), 16), &t_lbox));
+    CU(ws.buffer(11, std::max<size_t>(o.leaf_range.size() * 4, 16), &t_lrange));
+    CU(ws.buffer(12, std::max<size_t>(o.entry_tri.size() * 4, 16), &t_etri));
+    if ((rc = h2d(d_rec, h_vtx, n_rec * sizeof(Q4<T>))) || (rc = h2d(t_trec, h_trec, n_trec * sizeof(Q4<T>))) ||
+        (rc = h2d(d_thr, o.thr.data(), o.thr.size() * sizeof(T))) ||
+        (rc = h2d(t_cleaf, o.cell_leaf.data(), o.cell_leaf.size() * 4)) ||
+        (rc = h2d(t_lbox, o.leaf_box.data(), o.leaf_box.size() * sizeof(T))) ||
+        (rc = h2d(t_lrange, o.leaf_range.data(), o.leaf_range.size() * 4)) ||
+        (rc = h2d(t_etri, o.entry_tri.data(), o.entry_tri.size() * 4)))
         return rc;
     if (n_cell > 0)
         k_expand_cells<T><<<(int)std::min<long long>((n_cell + 255) / 256, 4096), 256, 0, d.stream>>>(
-            d_cleaf, d_lbox, d_lrange, n_cell, d_cell);
+            static_cast<const int32_t*>(t_cleaf), static_cast<const T*>(t_lbox), static_cast<const int32_t*>(t_lrange),
+            n_cell, d_cell);
     if (n_ent > 0)
         k_gather_entries<T><<<(int)std::min<long long>((n_ent * 5 + 255) / 256, 4096), 256, 0, d.stream>>>(
-            d_etri, d_trec, n_ent, d_ent);
+            static_cast<const int32_t*>(t_etri), static_cast<const Q4<T>*>(t_trec), n_ent, d_ent);
     CU(cudaGetLastError());
     d.S = Slots<T>{n, d_vtx, d_nrm, d_ctr, d_frgb, d_acc, d_db};
     Grid<T> G = grid_params(o, opt.walk_cap);
@@ -769,10 +819,16 @@ template <typename T>
 int download(DevImpl<T>& d, Scene<T>& s) {
     const int n = d.S.n;
     if (n != s.trinum) return fail(RAD_ERR_ARG, "scene slot count differs from the device copy");
-    std::vector<Q4<T>> acc((size_t)n * 3), db(n);
     CU(cudaSetDevice(d.device));
-    CU(cudaMemcpyAsync(acc.data(), d.S.accB, acc.size() * sizeof(Q4<T>), cudaMemcpyDeviceToHost, d.stream));
-    CU(cudaMemcpyAsync(db.data(), d.S.deltaB, db.size() * sizeof(Q4<T>), cudaMemcpyDeviceToHost, d.stream));
+    // through this thread's pinned staging: accB (3 records per slot), deltaB (1)
+    void* stage_p = nullptr;
+    CU(pinned_stage().get((size_t)n * 4 * sizeof(Q4<T>), &stage_p));
+    Q4<T>* acc = static_cast<Q4<T>*>(stage_p);
+    Q4<T>* db = acc + (size_t)n * 3;
+    if (n) {
+        CU(cudaMemcpyAsync(acc, d.S.accB, (size_t)n * 3 * sizeof(Q4<T>), cudaMemcpyDeviceToHost, d.stream));
+        CU(cudaMemcpyAsync(db, d.S.deltaB, (size_t)n * sizeof(Q4<T>), cudaMemcpyDeviceToHost, d.stream));
+    }
     CU(cudaStreamSynchronize(d.stream));
     for (int i = 0; i < n; i++) {
         Slot<T>& t = s.slots[i];
