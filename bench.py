@@ -206,7 +206,7 @@ def prepare_scenes(capi, gens, device, threads=None):
     from concurrent.futures import ThreadPoolExecutor
 
     def one(g):
-        o = capi.options_from_argv(g.argv())
+        o = capi.options_from_argv(g.argv(), jobs=_nproc())
         sc = capi.Scene.from_arrays(g.vtx, g.frgb, g.brgb, o)
         tr = capi.Octree(sc, device=device)
         sc.init(device=device)

@@ -31,9 +31,11 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <thread>
 #include <type_traits>
 #include <vector>
 
@@ -256,8 +258,8 @@ struct BatchImpl : BatchBase {
         *p = (U*)q;
         return RAD_OK;
     }
-    template <typename V>
-    int put(V** dst, const std::vector<V>& src) {
+    template <typename V, typename A>
+    int put(V** dst, const std::vector<V, A>& src) {
         int r = alloc(dst, src.size());
         if (r) return r;
         if (!src.empty()) {
@@ -393,31 +395,34 @@ int run(BatchImpl<T>& b, long long max_iters, long long* iters_done, int* n_acti
     return RAD_OK;
 }
 
-// One scene's compact arrays, appended to the batch's host staging vectors:
-// per-slot records, the thresholds, and the octree in the form the device
-// expands (a leaf per cell, leaf boxes and ranges, the triangle of each list
-// entry, one five-record group per triangle a list names).
-template <typename T>
-struct Staging {
-    std::vector<Q4<T>> vtx, nrm, ctr, frgb, acc, db, trec;
-    std::vector<T> thr, lbox;
-    std::vector<int32_t> cleaf, lrange, etri;
-};
+// The batch's host staging: per-slot records, the thresholds, and the octree
+// in the form the device expands (a leaf per cell, leaf boxes and ranges, the
+// triangle of each list entry, one five-record group per triangle a list
+// names), every scene at its own offsets.  The vectors are sized once with
+// zero pages that nothing writes until a scene's thread packs its range, so
+// the page faults of the first touch are spread over the packing threads.
+template <typename U>
+using StageVec = std::vector<U, ZeroPages<U>>;
 
 template <typename T>
-int stage_scene(const Scene<T>& s, const Octree<T>& o, Staging<T>& P, SceneOff& off) {
-    off.slot = (long long)P.frgb.size();
-    off.thr = (long long)P.thr.size();
-    off.cell = (long long)P.cleaf.size();
-    off.ent = (long long)P.etri.size();
-    off.lbox = (long long)P.lbox.size() / 8;
-    off.lrange = (long long)P.lrange.size() / 2;
-    off.trec = (long long)P.trec.size() / 5;
-    off.n = s.trinum;
-    const size_t n = (size_t)s.trinum;
-    const size_t b3 = P.vtx.size(), b1 = P.frgb.size();
-    P.vtx.resize(b3 + 3 * n); P.acc.resize(b3 + 3 * n);
-    P.nrm.resize(b1 + n); P.ctr.resize(b1 + n); P.frgb.resize(b1 + n); P.db.resize(b1 + n);
+struct Staging {
+    StageVec<Q4<T>> vtx, nrm, ctr, frgb, acc, db, trec;
+    StageVec<T> thr, lbox;
+    StageVec<int32_t> cleaf, lrange, etri;
+};
+
+// the triangles scene s's lists name: 0 .. n_tri-1 (-1: a list names a triangle beyond the scene)
+template <typename T>
+int list_triangles(const Scene<T>& s, const Octree<T>& o) {
+    int n_tri = 0;
+    for (int32_t id : o.entry_tri) n_tri = std::max(n_tri, id + 1);
+    return n_tri > s.trinum ? -1 : n_tri;
+}
+
+// pack scene s into its ranges of the staging (offsets already set in off)
+template <typename T>
+void stage_scene(const Scene<T>& s, const Octree<T>& o, int n_tri, Staging<T>& P, const SceneOff& off) {
+    const size_t n = (size_t)s.trinum, b3 = (size_t)off.slot * 3, b1 = (size_t)off.slot;
     for (size_t i = 0; i < n; i++) {
         const Slot<T>& t = s.slots[i];
         for (int v = 0; v < 3; v++) {
@@ -431,11 +436,7 @@ int stage_scene(const Scene<T>& s, const Octree<T>& o, Staging<T>& P, SceneOff& 
         P.db[b1 + i] = {t.deltaB[0], t.deltaB[1], t.deltaB[2], 0};
     }
     // the walk's triangle records (as RayHitted reads TriStore at shooting time)
-    int n_tri = 0;
-    for (int32_t id : o.entry_tri) n_tri = std::max(n_tri, id + 1);
-    if (n_tri > s.trinum) return fail(RAD_ERR_ARG, "octree names a triangle beyond the scene");
-    const size_t bt = P.trec.size();
-    P.trec.resize(bt + 5 * (size_t)n_tri);
+    const size_t bt = (size_t)off.trec * 5;
     for (int id = 0; id < n_tri; id++) {
         const Slot<T>& t = s.slots[id];
         Q4<T>* r = &P.trec[bt + 5 * (size_t)id];
@@ -444,12 +445,27 @@ int stage_scene(const Scene<T>& s, const Octree<T>& o, Staging<T>& P, SceneOff& 
         for (int e = 0; e < 3; e++) r[2 + e] = {t.se[e][0], t.se[e][1], t.se[e][2], t.se[e][3]};
     }
     // indices stay scene-local: the expansion kernels run per scene on offset pointers
-    P.cleaf.insert(P.cleaf.end(), o.cell_leaf.begin(), o.cell_leaf.end());
-    P.lbox.insert(P.lbox.end(), o.leaf_box.begin(), o.leaf_box.end());
-    P.lrange.insert(P.lrange.end(), o.leaf_range.begin(), o.leaf_range.end());
-    P.etri.insert(P.etri.end(), o.entry_tri.begin(), o.entry_tri.end());
-    P.thr.insert(P.thr.end(), o.thr.begin(), o.thr.end());
-    return RAD_OK;
+    std::copy(o.cell_leaf.begin(), o.cell_leaf.end(), P.cleaf.begin() + off.cell);
+    std::copy(o.leaf_box.begin(), o.leaf_box.end(), P.lbox.begin() + off.lbox * 8);
+    std::copy(o.leaf_range.begin(), o.leaf_range.end(), P.lrange.begin() + off.lrange * 2);
+    std::copy(o.entry_tri.begin(), o.entry_tri.end(), P.etri.begin() + off.ent);
+    std::copy(o.thr.begin(), o.thr.end(), P.thr.begin() + off.thr);
+}
+
+// run f(0..n-1) on up to `jobs` host threads (scenes taken from a shared counter)
+template <typename F>
+void parallel_scenes(int n, int jobs, F f) {
+    std::atomic<int> next{0};
+    auto worker = [&]() {
+        for (int k; (k = next.fetch_add(1)) < n;) f(k);
+    };
+    std::vector<std::thread> pool;
+    try {
+        for (int j = 1; j < jobs; j++) pool.emplace_back(worker);
+    } catch (...) {   // threads that could not start: the others take their scenes
+    }
+    worker();
+    for (auto& th : pool) th.join();
 }
 
 template <typename T>
@@ -479,17 +495,41 @@ int batch_create(const rad_scene* const* scenes, const rad_octree* const* trees,
     b.trace_cap = trace_cap;
     CU(cudaSetDevice(device));
     CU(cudaStreamCreateWithFlags(&b.stream, cudaStreamNonBlocking));
-    Staging<T> P;
+    // offsets of every scene in the staging, then the packing on the -jobs threads
+    const int jobs = std::max(1, std::min(opts[0].jobs, 16));
+    std::vector<int> n_tri(n_scenes);
+    parallel_scenes(n_scenes, jobs, [&](int s) { n_tri[s] = list_triangles(scene_of<T>(scenes[s]), tree_of<T>(trees[s])); });
     b.off.resize(n_scenes);
     long long total_groups = 0;
-    int rc;
+    SceneOff end;
     for (int s = 0; s < n_scenes; s++) {
-        if ((rc = stage_scene(scene_of<T>(scenes[s]), tree_of<T>(trees[s]), P, b.off[s]))) return rc;
-        total_groups += (b.off[s].n + kSlotsPerWarp - 1) / kSlotsPerWarp;
+        if (n_tri[s] < 0) return fail(RAD_ERR_ARG, "octree names a triangle beyond the scene");
+        const Scene<T>& sc = scene_of<T>(scenes[s]);
+        const Octree<T>& tr = tree_of<T>(trees[s]);
+        SceneOff& o = b.off[s];
+        o = end;
+        o.n = sc.trinum;
+        end.slot += sc.trinum;
+        end.trec += n_tri[s];
+        end.cell += (long long)tr.cell_leaf.size();
+        end.lbox += (long long)tr.leaf_box.size() / 8;
+        end.lrange += (long long)tr.leaf_range.size() / 2;
+        end.ent += (long long)tr.entry_tri.size();
+        end.thr += (long long)tr.thr.size();
+        total_groups += (o.n + kSlotsPerWarp - 1) / kSlotsPerWarp;
     }
-    if (total_groups > 0x7fffffffLL || (long long)trace_cap * n_scenes * b.P > 0x7fffffffLL ||
-        (long long)P.frgb.size() > 0x7fffffffLL)
+    if (total_groups > 0x7fffffffLL || (long long)trace_cap * n_scenes * b.P > 0x7fffffffLL || end.slot > 0x7fffffffLL)
         return fail(RAD_ERR_CAPACITY, "batch too large");
+    Staging<T> P;
+    P.vtx.resize((size_t)end.slot * 3); P.acc.resize((size_t)end.slot * 3);
+    P.nrm.resize((size_t)end.slot); P.ctr.resize((size_t)end.slot); P.frgb.resize((size_t)end.slot);
+    P.db.resize((size_t)end.slot); P.trec.resize((size_t)end.trec * 5);
+    P.cleaf.resize((size_t)end.cell); P.lbox.resize((size_t)end.lbox * 8); P.lrange.resize((size_t)end.lrange * 2);
+    P.etri.resize((size_t)end.ent); P.thr.resize((size_t)end.thr);
+    parallel_scenes(n_scenes, jobs, [&](int s) {
+        stage_scene(scene_of<T>(scenes[s]), tree_of<T>(trees[s]), n_tri[s], P, b.off[s]);
+    });
+    int rc;
     Q4<T> *d_vtx, *d_nrm, *d_ctr, *d_frgb, *d_acc, *d_db, *d_trec, *d_ent;
     CellRec<T>* d_cell;
     T *d_thr, *d_lbox;

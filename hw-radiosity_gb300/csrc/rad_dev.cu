@@ -58,7 +58,7 @@ namespace dev {
 // fraction of the step (an item that was already split: the second figure)
 constexpr double kHeavyFrac = 0.55, kHeavyFracSplit = 0.27;
 // ... and longer than this multiple of the step's mean group time
-constexpr double kHeavyMeanMult = 2.5;
+constexpr double kHeavyMeanMult = 3.0;
 // a group shot whole that took longer than this multiple of the step's mean
 // group time starts early in the next step
 constexpr double kEarlyMeanMult = 1.5;

@@ -354,7 +354,7 @@ class Device:
     def set_counting(self, on: bool):
         _check(load().rad_dev_set_counting(self.h, 1 if on else 0))
 
-    def set_schedule(self, split_frac=0.55, split_frac_split=0.27, split_mean_mult=2.5, early_mean_mult=1.5):
+    def set_schedule(self, split_frac=0.55, split_frac_split=0.27, split_mean_mult=3.0, early_mean_mult=1.5):
         """Limits of the single-shooter schedule (rad_dev_set_schedule); all 0
         splits every group after the first step."""
         _check(load().rad_dev_set_schedule(self.h, split_frac, split_frac_split, split_mean_mult, early_mean_mult))

@@ -197,7 +197,7 @@ int rad_dev_stats(const rad_dev* d, rad_stats* st);
  * is shot in the next as 2-slot items with 4 lanes per corner; an item that
  * was already split stays split above split_frac_split * step time; a group
  * over early_mean_mult * mean group time is handed out first.  Defaults
- * 0.55, 0.27, 2.5, 1.5.  All zero splits every group after the first step
+ * 0.55, 0.27, 3.0, 1.5.  All zero splits every group after the first step
  * (tests use this to run the 4-lane walk everywhere); large values turn it
  * off. */
 int rad_dev_set_schedule(rad_dev* d, double split_frac, double split_frac_split, double split_mean_mult,
