@@ -22,8 +22,11 @@
 //      not written by a split earlier in this step, the shooter slot was not
 //      either, and (for sample points) the stream is at the triple the value
 //      was drawn from.  When a sample loop broke early or a rewritten receiver
-//      drew points, the next receiver that samples starts a new speculation
-//      from the stream's position (another k_adapt_samples launch).  Values
+//      drew points, a new speculation starts from the next receiver's first
+//      point at the stream's position as soon as the receiver is done
+//      (another k_adapt_samples launch, which stops the one before it).  The
+//      host takes the points the device has written by the time it needs
+//      them and never waits for one.  Points not written yet, and values
 //      whose inputs changed -- rewritten or appended receivers, re-shaded
 //      neighbours -- are evaluated on the host with the same walk and
 //      form-factor code (it is compiled for both).
@@ -178,17 +181,23 @@ __global__ void __launch_bounds__(kScanTile) k_scan_add(const long long* tile_of
 // receiver (largest s with toff[s] <= t), GetPointInTriangle (shade.cpp:49-68)
 // and the point's AdaptCalFF(CalFF(...)) (shade.cpp:499-502).  Written to host
 // memory: ff[t] and the walk counters of its rays (rays | capped << 8 |
-// loops << 16), added on the host only for points it uses.
+// loops << 16), added on the host only for points it uses, then, after a
+// system-scope fence, tag[t] = gen: the host reads a point as soon as its tag
+// shows this speculation, without waiting for the kernel.  A thread stops
+// when *live (host memory the host writes) no longer holds gen: the host has
+// started a newer speculation and will not read this one's points.
 template <typename T>
 __global__ void k_adapt_samples(Slots<T> S, Grid<T> G, const Shooter<T>* __restrict__ shp,
                                 const long long* __restrict__ toff, int n, long long start, long long end,
                                 long long base, const int32_t* __restrict__ ring, long long ring_len,
-                                T* __restrict__ out_ff, int* __restrict__ out_code) {
+                                T* __restrict__ out_ff, int* __restrict__ out_code, unsigned* out_tag,
+                                const volatile unsigned* live, unsigned gen) {
     const long long total = toff[n];
     if (end > total) end = total;
     const Shooter<T> sh = *shp;
     for (long long t = start + blockIdx.x * (long long)blockDim.x + threadIdx.x; t < end;
          t += (long long)gridDim.x * blockDim.x) {
+        if (*live != gen) return;
         int lo = 0, hi = n - 1;        // toff is non-decreasing; toff[0] = 0 <= t
         while (lo < hi) {
             const int mid = (lo + hi + 1) >> 1;
@@ -208,6 +217,8 @@ __global__ void k_adapt_samples(Slots<T> S, Grid<T> G, const Shooter<T>* __restr
         Cnt c = {0, 0, 0, 0, 0, 0, 0, 0};
         out_ff[t] = corner_ff<T, false>(sh, pt, nd, nn.w, (int)S.frgb[s].w, G, c);
         out_code[t] = (int)(c.rays | (c.capped << 8) | (c.loops << 16));
+        __threadfence_system();
+        *(volatile unsigned*)(out_tag + t) = gen;
     }
 }
 
@@ -339,8 +350,12 @@ struct AdaptImpl {
     // [sp_start, sp_end) drawn from rand() triples sp_base + (t - sp_start).
     // The host uses a receiver's speculated values only when its draws start
     // at exactly that triple; a sample loop that breaks early or a rewritten
-    // receiver that draws moves the stream, and the next receiver that samples
-    // starts a new speculation from its own position.
+    // receiver that draws moves the stream, and a new speculation starts from
+    // the next receiver's first point at the stream's position.  Speculations
+    // are numbered (sp_gen); the kernel tags each point it writes with its
+    // number (h_stag) and stops once *h_live names a newer one.  The host
+    // takes a point the kernel has already written and evaluates the others
+    // itself, and a superseded speculation frees the GPU at once.
     uint8_t* d_open = nullptr;
     uint8_t* h_open = nullptr;            // pinned
     long long *d_ntask = nullptr, *d_toff = nullptr, *d_tiles = nullptr;
@@ -356,11 +371,19 @@ struct AdaptImpl {
     int32_t* h_ring = nullptr;            // pinned staging of the ring
     long long ring_len = 1 << 21, ring_hi = 0;
     long long sp_start = 0, sp_end = 0, sp_base = 0;
+    unsigned* h_stag = nullptr;           // mapped: the speculation that wrote each point
+    unsigned* h_live = nullptr;           // mapped: the speculation whose points are still wanted
+    unsigned* dm_stag = nullptr;
+    unsigned* dm_live = nullptr;
+    unsigned sp_gen = 0;
+    cudaEvent_t copies_done = nullptr;    // the step's test results are on the host
     long long dev_samples = 0, spec_launches = 0, split_candidates = 0;
     std::vector<void*> pinned;
 
     ~AdaptImpl() {
+        if (h_live) __atomic_store_n(h_live, sp_gen + 1, __ATOMIC_RELEASE);   // stop a running speculation
         if (stream) cudaStreamSynchronize(stream);
+        if (copies_done) cudaEventDestroy(copies_done);
         for (void* p : allocs) cudaFree(p);
         for (void* p : pinned) cudaFreeHost(p);
         if (stream) cudaStreamDestroy(stream);
@@ -464,10 +487,17 @@ int adapt_create(Scene<T>& s, const Octree<T>& o, const rad_options& opt, int de
         (rc = a.host_alloc(&a.h_nsplit, 1, cudaHostAllocDefault)) ||
         (rc = a.host_alloc(&a.h_ring, (size_t)a.ring_len, cudaHostAllocDefault)) ||
         (rc = a.host_alloc(&a.h_sff, (size_t)a.task_cap, cudaHostAllocMapped)) ||
-        (rc = a.host_alloc(&a.h_scode, (size_t)a.task_cap, cudaHostAllocMapped)))
+        (rc = a.host_alloc(&a.h_scode, (size_t)a.task_cap, cudaHostAllocMapped)) ||
+        (rc = a.host_alloc(&a.h_stag, (size_t)a.task_cap, cudaHostAllocMapped)) ||
+        (rc = a.host_alloc(&a.h_live, 1, cudaHostAllocMapped)))
         return rc;
     CU(cudaHostGetDevicePointer((void**)&a.dm_sff, a.h_sff, 0));
     CU(cudaHostGetDevicePointer((void**)&a.dm_scode, a.h_scode, 0));
+    CU(cudaHostGetDevicePointer((void**)&a.dm_stag, a.h_stag, 0));
+    CU(cudaHostGetDevicePointer((void**)&a.dm_live, a.h_live, 0));
+    std::memset(a.h_stag, 0, (size_t)a.task_cap * sizeof(unsigned));
+    *a.h_live = 0;
+    CU(cudaEventCreateWithFlags(&a.copies_done, cudaEventDisableTiming));
     a.ff.assign((size_t)a.cap * 4, (T)0);
     a.mod_step.assign((size_t)a.cap, 0);
     a.dirty.assign((size_t)a.cap, 0);
@@ -495,12 +525,30 @@ int ring_top_up(AdaptImpl<T>& a) {
     return RAD_OK;
 }
 
+// stop every speculation in flight: none of their points will be read
+template <typename T>
+int spec_cancel(AdaptImpl<T>& a) {
+    if (a.sp_gen >= 0xfffffff0u) {      // numbers about to wrap: clear the tags first
+        CU(cudaStreamSynchronize(a.stream));
+        std::memset(a.h_stag, 0, (size_t)a.task_cap * sizeof(unsigned));
+        a.sp_gen = 0;
+    }
+    a.sp_gen++;
+    __atomic_store_n(a.h_live, a.sp_gen, __ATOMIC_RELEASE);
+    a.sp_start = a.sp_end = a.sp_base = 0;
+    return RAD_OK;
+}
+
 // enqueue the sample points of tasks [start, ...) drawn from triples base, ...
-// (clipped to the task capacity, the ring and, on the device, the step's total)
+// (clipped to the task capacity, the ring and, on the device, the step's
+// total), superseding the speculation in flight.  The ring's staging may be
+// rewritten while an older copy from it is still queued: that copy then moves
+// the newer values, which land in the same ring positions, and only the
+// superseded kernel before it could read them.
 template <typename T>
 int spec_enqueue(AdaptImpl<T>& a, const Slots<T>& S, int n0, long long start, long long base, long long end) {
     int rc;
-    if ((rc = ring_top_up(a))) return rc;
+    if ((rc = spec_cancel(a)) || (rc = ring_top_up(a))) return rc;
     end = std::min(end, a.task_cap);
     end = std::min(end, start + (a.rng.pos + a.ring_len) / 3 - base);
     a.sp_start = start;
@@ -511,9 +559,21 @@ int spec_enqueue(AdaptImpl<T>& a, const Slots<T>& S, int n0, long long start, lo
     const long long work = a.sp_end - start;
     const int blocks = (int)std::max<long long>(1, std::min<long long>((work + 127) / 128, 152 * 16));
     k_adapt_samples<T><<<blocks, 128, 0, a.stream>>>(S, a.Gd, a.d_sh, a.d_toff, n0, start, a.sp_end, base, a.d_ring,
-                                                     a.ring_len, a.dm_sff, a.dm_scode);
+                                                     a.ring_len, a.dm_sff, a.dm_scode, a.dm_stag, a.dm_live,
+                                                     a.sp_gen);
     CU(cudaGetLastError());
     return RAD_OK;
+}
+
+// Whether point t of the current speculation is on the host.  The host never
+// waits for one: a walk on the GPU takes longer than the same walk on the
+// host, so a point the device has not written yet is evaluated on the host
+// (the same arithmetic, the same value) while the kernel runs ahead to the
+// receivers after it.  A failed kernel is reported by the next step's stream
+// synchronisation.
+template <typename T>
+bool spec_ready(const AdaptImpl<T>& a, long long t) {
+    return __atomic_load_n(a.h_stag + t, __ATOMIC_ACQUIRE) == a.sp_gen;
 }
 
 template <typename T>
@@ -546,27 +606,39 @@ struct StepCtx {
     Shooter<T> sh;            // the shooter as the precompute saw it
     Shooter<T> live;          // rebuilt from the slot after a split rewrote it
 
-    // The device's form factors of receiver d's n sample points, when they are
-    // the ones it draws now: d is unchanged this step (pre_ok), the device's
-    // test gave it n points, and the speculation covering them starts them at
-    // the stream's current triple.  Otherwise a new speculation starts at d.
-    // Null when d's points are evaluated on the host.
-    const T* device_points(int d, int n, const int** codes) {
-        if (a.rng.pos % 3 != 0) return nullptr;
+    // whether the current speculation holds points [t, t + n) drawn from the
+    // triples that start at triple cur
+    bool covered(long long t, long long n, long long cur) const {
+        return t >= a.sp_start && t + n <= a.sp_end && a.sp_base + (t - a.sp_start) == cur;
+    }
+
+    // The first task of receiver d's n sample points on the device, when they
+    // are the ones it draws now: d is unchanged this step (pre_ok), the
+    // device's test gave it n points, and the speculation covering them starts
+    // them at the stream's current triple (otherwise a new speculation starts
+    // at d).  -1 when d's points are evaluated on the host.
+    long long device_points(int d, int n) {
+        if (a.rng.pos % 3 != 0) return -1;
         const long long t0 = a.h_toff[d];
-        if (a.h_toff[d + 1] - t0 != n) return nullptr;
+        if (a.h_toff[d + 1] - t0 != n) return -1;
         const long long cur = a.rng.pos / 3;
-        auto covered = [&]() {
-            return t0 >= a.sp_start && t0 + n <= a.sp_end && a.sp_base + (t0 - a.sp_start) == cur;
-        };
-        if (!covered()) {
-            int rc = spec_enqueue(a, S, n0, t0, cur, a.h_toff[n0]);
-            if (!rc && cudaStreamSynchronize(a.stream) != cudaSuccess) rc = fail(RAD_ERR_CUDA, "sample-point kernel failed");
-            if (rc) { err = rc; return nullptr; }
-            if (!covered()) return nullptr;
+        if (!covered(t0, n, cur)) {
+            if (int rc = spec_enqueue(a, S, n0, t0, cur, a.h_toff[n0])) { err = rc; return -1; }
+            if (!covered(t0, n, cur)) return -1;
         }
-        *codes = a.h_scode + t0;
-        return a.h_sff + t0;
+        return t0;
+    }
+
+    // After receiver d is done: when the stream no longer sits where the
+    // speculation puts the next receiver's first point (d broke its sample
+    // loop, drew on the host, or drew nothing where the device's test said it
+    // would), start the speculation from there now, so that it runs while the
+    // host gets to that receiver.
+    void respeculate_after(int d) {
+        if (d + 1 >= n0 || a.rng.pos % 3 != 0) return;
+        const long long t = a.h_toff[d + 1];
+        if (t >= a.h_toff[n0] || covered(t, 1, a.rng.pos / 3)) return;
+        if (int rc = spec_enqueue(a, S, n0, t, a.rng.pos / 3, a.h_toff[n0])) err = rc;
     }
 
     // AdaptCalFF(CalFF(...)) for point p of receiver d (its normal) with ban logdes
@@ -601,8 +673,7 @@ struct StepCtx {
         T dff;
         if ((dff = (T)std::fabs((double)(ground - ffs))) < o.delta_ff) {
             const int n = (int)(des.area / o.sample_area);
-            const int* codes = nullptr;
-            const T* dev = pre && n > 0 ? device_points(d, n, &codes) : nullptr;
+            const long long t0 = pre && n > 0 ? device_points(d, n) : -1;
             for (int k = 0; k < n; k++) {
                 // GetPointInTriangle, shade.cpp:49-68
                 T r1 = (T)a.rng.next(), r2 = (T)a.rng.next(), r3 = (T)a.rng.next();
@@ -610,11 +681,12 @@ struct StepCtx {
                 r1 /= tot; r2 /= tot; r3 /= tot;
                 ground = r1 * f[0] + r2 * f[1] + r3 * f[2];
                 a.samples++;
-                if (dev) {      // drawn from this very triple on the device
-                    ffs = dev[k];
-                    a.hc.rays += codes[k] & 0xff;
-                    a.hc.capped += (codes[k] >> 8) & 0xff;
-                    a.hc.loops += (codes[k] >> 16) & 0xff;
+                if (t0 >= 0 && spec_ready(a, t0 + k)) {   // drawn from this very triple on the device
+                    const int code = a.h_scode[t0 + k];
+                    ffs = a.h_sff[t0 + k];
+                    a.hc.rays += code & 0xff;
+                    a.hc.capped += (code >> 8) & 0xff;
+                    a.hc.loops += (code >> 16) & 0xff;
                     a.dev_samples++;
                 } else {
                     T pt[3];
@@ -664,14 +736,13 @@ int adapt_step(AdaptImpl<T>& a) {
     if (src < 0) { a.done = true; return RAD_OK; }
     a.trace.push_back(src);
     int rc;
-    if ((rc = adapt_upload_dirty(a))) return rc;
+    if ((rc = spec_cancel(a)) || (rc = adapt_upload_dirty(a))) return rc;
     const int n0 = s.trinum;
     const Slots<T> S{n0, a.d_vtx, a.d_nrm, a.d_ctr, a.d_frgb, nullptr, nullptr};
     StepCtx<T> cx{a, src, s.slots[src].parent, n0, S};
     host_shooter(s.slots[src], src, cx.logsrc, cx.sh);
     CU(cudaMemcpyAsync(a.d_sh, &cx.sh, sizeof cx.sh, cudaMemcpyHostToDevice, a.stream));
     a.h_toff[0] = 0;
-    a.sp_start = a.sp_end = a.sp_base = 0;
     if (n0 > 0) {
         // the receivers the loop will visit, as the step starts
         for (int d = 0; d < n0; d++) {
@@ -693,17 +764,19 @@ int adapt_step(AdaptImpl<T>& a) {
         k_scan_sums<<<1, kScanTile, 0, a.stream>>>(a.d_tiles, tiles, a.d_toff, n0);
         k_scan_add<<<tiles, kScanTile, 0, a.stream>>>(a.d_tiles, n0, a.d_toff);
         CU(cudaGetLastError());
-        // the first speculation: every sample point of the step, as if none broke early
-        int rc0;
-        if (a.rng.pos % 3 == 0 && (rc0 = spec_enqueue(a, S, n0, 0, a.rng.pos / 3, a.task_cap))) return rc0;
         CU(cudaMemcpyAsync(a.ff.data(), a.d_ff, (size_t)n0 * 4 * sizeof(T), cudaMemcpyDeviceToHost, a.stream));
         CU(cudaMemcpyAsync(a.h_toff, a.d_toff, (size_t)(n0 + 1) * sizeof(long long), cudaMemcpyDeviceToHost, a.stream));
         CU(cudaMemcpyAsync(a.h_nsplit, a.d_nsplit, sizeof(unsigned), cudaMemcpyDeviceToHost, a.stream));
-    }
-    CU(cudaStreamSynchronize(a.stream));
-    if (n0 > 0) {
+        CU(cudaEventRecord(a.copies_done, a.stream));
+        // the first speculation: every sample point of the step, as if none
+        // broke early; it runs while the host starts the receiver loop
+        int rc0;
+        if (a.rng.pos % 3 == 0 && (rc0 = spec_enqueue(a, S, n0, 0, a.rng.pos / 3, a.task_cap))) return rc0;
+        CU(cudaEventSynchronize(a.copies_done));
         a.sp_end = std::min(a.sp_end, a.h_toff[n0]);
         a.split_candidates += *a.h_nsplit;
+    } else {
+        CU(cudaStreamSynchronize(a.stream));
     }
     // serialRadiosity's receiver loop, rad.cpp:464-485 (bound re-read: splits append slots)
     for (int d = 0; d < s.trinum; d++) {
@@ -712,8 +785,11 @@ int adapt_step(AdaptImpl<T>& a) {
         if (t.parent < 0) continue;
         if (!is_open(t)) continue;
         if (cx.shade(d, t.parent)) d--;
+        else cx.respeculate_after(d);
         if (cx.err) return cx.err;
     }
+    int rc1;
+    if ((rc1 = spec_cancel(a))) return rc1;
     Slot<T>& sr = s.slots[src];
     sr.deltaB[0] = sr.deltaB[1] = sr.deltaB[2] = 0;
     a.steps++;
