@@ -31,15 +31,14 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
-#include <atomic>
 #include <cstdio>
 #include <cstring>
 #include <string>
-#include <thread>
 #include <type_traits>
 #include <vector>
 
 #include "capi_internal.h"
+#include "prep_workspace.h"
 #include "rad_kernels.cuh"
 
 namespace radgb {
@@ -235,6 +234,7 @@ struct BatchImpl : BatchBase {
     std::vector<int> done;               // host mirror, per scene
     std::vector<long long> steps;        // steps shot, per scene
     cudaGraphExec_t graphs[3][2][33] = {};   // [form][counting][iterations per launch]
+    bool graph_seen[3][2][33] = {};          // a chunk of that shape has run once
     cudaEvent_t ev[2] = {nullptr, nullptr};
 
     ~BatchImpl() override {
@@ -296,9 +296,19 @@ int launch_iter(BatchImpl<T>& b, cudaStream_t s) {
     return b.counting ? launch_shoot_form<T, true, false, false>(b, s) : launch_shoot_form<T, false, false, false>(b, s);
 }
 
+// The graph of a chunk of `iters` iterations, built the second time a chunk
+// of that shape runs; null the first time, when the caller launches the
+// iterations one by one (they overlap the device's work; a capture would
+// delay it).
 template <typename T>
 int graph_for(BatchImpl<T>& b, int iters, cudaGraphExec_t* out) {
     cudaGraphExec_t& slot = b.graphs[b.form][b.counting ? 1 : 0][iters];
+    bool& seen = b.graph_seen[b.form][b.counting ? 1 : 0][iters];
+    if (!slot && !seen) {
+        seen = true;
+        *out = nullptr;
+        return RAD_OK;
+    }
     if (!slot) {
         cudaGraph_t g;
         CU(cudaStreamBeginCapture(b.stream, cudaStreamCaptureModeThreadLocal));
@@ -375,7 +385,12 @@ int run(BatchImpl<T>& b, long long max_iters, long long* iters_done, int* n_acti
         cudaGraphExec_t g;
         if ((rc = graph_for(b, chunk, &g))) return rc;
         if (ms) CU(cudaEventRecord(b.ev[0], b.stream));
-        CU(cudaGraphLaunch(g, b.stream));
+        if (g) {
+            CU(cudaGraphLaunch(g, b.stream));
+        } else {
+            for (int k = 0; k < chunk; k++)
+                if ((rc = launch_iter(b, b.stream))) return rc;
+        }
         if (ms) CU(cudaEventRecord(b.ev[1], b.stream));
         bool changed = false;
         if ((rc = refresh(b, &changed))) return rc;
@@ -452,22 +467,6 @@ void stage_scene(const Scene<T>& s, const Octree<T>& o, int n_tri, Staging<T>& P
     std::copy(o.thr.begin(), o.thr.end(), P.thr.begin() + off.thr);
 }
 
-// run f(0..n-1) on up to `jobs` host threads (scenes taken from a shared counter)
-template <typename F>
-void parallel_scenes(int n, int jobs, F f) {
-    std::atomic<int> next{0};
-    auto worker = [&]() {
-        for (int k; (k = next.fetch_add(1)) < n;) f(k);
-    };
-    std::vector<std::thread> pool;
-    try {
-        for (int j = 1; j < jobs; j++) pool.emplace_back(worker);
-    } catch (...) {   // threads that could not start: the others take their scenes
-    }
-    worker();
-    for (auto& th : pool) th.join();
-}
-
 template <typename T>
 const Scene<T>& scene_of(const rad_scene* s);
 template <>
@@ -498,7 +497,7 @@ int batch_create(const rad_scene* const* scenes, const rad_octree* const* trees,
     // offsets of every scene in the staging, then the packing on the -jobs threads
     const int jobs = std::max(1, std::min(opts[0].jobs, 16));
     std::vector<int> n_tri(n_scenes);
-    parallel_scenes(n_scenes, jobs, [&](int s) { n_tri[s] = list_triangles(scene_of<T>(scenes[s]), tree_of<T>(trees[s])); });
+    for_each_item(n_scenes, jobs, [&](int s) { n_tri[s] = list_triangles(scene_of<T>(scenes[s]), tree_of<T>(trees[s])); });
     b.off.resize(n_scenes);
     long long total_groups = 0;
     SceneOff end;
@@ -526,7 +525,7 @@ int batch_create(const rad_scene* const* scenes, const rad_octree* const* trees,
     P.db.resize((size_t)end.slot); P.trec.resize((size_t)end.trec * 5);
     P.cleaf.resize((size_t)end.cell); P.lbox.resize((size_t)end.lbox * 8); P.lrange.resize((size_t)end.lrange * 2);
     P.etri.resize((size_t)end.ent); P.thr.resize((size_t)end.thr);
-    parallel_scenes(n_scenes, jobs, [&](int s) {
+    for_each_item(n_scenes, jobs, [&](int s) {
         stage_scene(scene_of<T>(scenes[s]), tree_of<T>(trees[s]), n_tri[s], P, b.off[s]);
     });
     int rc;

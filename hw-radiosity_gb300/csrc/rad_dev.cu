@@ -34,7 +34,6 @@
 #include <cstring>
 #include <mutex>
 #include <string>
-#include <thread>
 #include <type_traits>
 #include <vector>
 
@@ -455,6 +454,7 @@ struct DevImpl : DevBase {
     double* d_unshot = nullptr;   // kUnshotCtas partials, then the total
     int* d_trace = nullptr;
     long long trace_cap = 0;
+    bool trace_own = false;   // d_trace is its own allocation (after a growth), not part of the block
     int n_cta = 0;          // CTAs of the current layout's kernel
     int n_cta1 = 0, n_cta2 = 0;
     int n_cta_nf = 0;       // the counting kernels and the several-shooters kernel (3 CTAs per SM)
@@ -464,6 +464,7 @@ struct DevImpl : DevBase {
     T conv = 0;
     bool counting = false;
     cudaGraphExec_t graphs[3][2][33] = {};   // [layout][counting][steps per launch]
+    bool graph_seen[3][2][33] = {};          // a chunk of that shape has run once
     cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
     std::vector<void*> allocs;
     size_t bytes = 0;
@@ -478,8 +479,17 @@ struct DevImpl : DevBase {
         for (auto& e : ev)
             if (e) cudaEventDestroy(e);
         for (void* p : allocs) cudaFree(p);
-        if (d_trace) cudaFree(d_trace);
+        if (d_trace && trace_own) cudaFree(d_trace);
         if (stream) cudaStreamDestroy(stream);
+    }
+    // one cudaMalloc for every array of a DevBlock, carved at its offsets
+    int alloc_block(DevBlock& b) {
+        void* q = nullptr;
+        CU(cudaMalloc(&q, std::max<size_t>(b.size, 16)));
+        allocs.push_back(q);
+        bytes += b.size;
+        b.carve(q);
+        return RAD_OK;
     }
     template <typename U>
     int alloc(U** p, size_t count) {
@@ -496,6 +506,72 @@ struct DevImpl : DevBase {
     size_t shoot_smem() const { return kMaxShooterBytes<T>(P) + (size_t)n_thr * sizeof(T); }
 };
 
+// 1 + the largest triangle a list entry names (0 without entries), the
+// entries split over the host pool when there are many
+inline int max_entry_tri(const std::vector<int32_t>& ent, int jobs) {
+    const int n = (int)ent.size();
+    const int parts = pack_jobs(n, jobs);
+    std::vector<int> best((size_t)parts, 0);
+    split_range(parts, parts, [&](int a, int b) {
+        for (int k = a; k < b; k++) {
+            int m = 0;
+            const int lo = (int)((long long)n * k / parts), hi = (int)((long long)n * (k + 1) / parts);
+            for (int i = lo; i < hi; i++) m = std::max(m, ent[(size_t)i] + 1);
+            best[(size_t)k] = m;
+        }
+    });
+    return parts ? *std::max_element(best.begin(), best.end()) : 0;
+}
+
+// Resident CTAs per SM of each k_shoot form at a dynamic shared memory size,
+// and the SM count: the same for every handle of a device and size, so kept
+// for the process (with the kernels' shared-memory limits raised once per
+// device), not queried again at each handle's creation.
+struct ShootShape {
+    int sms = 0, per1 = 0, per_nf = 0, per2 = 0;
+};
+
+template <typename T>
+int shoot_shape(int device, size_t smem, ShootShape* out) {
+    struct Known {
+        int device;
+        size_t smem;
+        ShootShape shape;
+    };
+    static std::mutex m;
+    static std::vector<Known> known;
+    static std::vector<size_t> smem_allowed;   // per device: the kernels' dynamic shared memory limit
+    std::lock_guard<std::mutex> g(m);
+    for (const Known& k : known)
+        if (k.device == device && k.smem == smem) {
+            *out = k.shape;
+            return RAD_OK;
+        }
+    if ((int)smem_allowed.size() <= device) smem_allowed.resize((size_t)device + 1, 48 * 1024);
+    if (smem > smem_allowed[(size_t)device]) {
+        CU(cudaFuncSetAttribute(k_shoot<T, false, false, 3, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        CU(cudaFuncSetAttribute(k_shoot<T, true, false, 3, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        CU(cudaFuncSetAttribute(k_shoot<T, false, true, kForm1MinBlocks<T>, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)smem));
+        CU(cudaFuncSetAttribute(k_shoot<T, true, true, 3, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        if constexpr (std::is_same<T, float>::value)
+            CU(cudaFuncSetAttribute(k_shoot<T, false, true, 4, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        smem_allowed[(size_t)device] = smem;
+    }
+    ShootShape sh;
+    CU(cudaDeviceGetAttribute(&sh.sms, cudaDevAttrMultiProcessorCount, device));
+    CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&sh.per1, k_shoot<T, false, true, kForm1MinBlocks<T>, 4>,
+                                                     kShootThreads, smem));
+    CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&sh.per_nf, k_shoot<T, false, false, 3, 4>, kShootThreads, smem));
+    if constexpr (std::is_same<T, float>::value)
+        CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&sh.per2, k_shoot<T, false, true, 4, 1>, kShootThreads, smem));
+    else
+        sh.per2 = sh.per1;
+    known.push_back({device, smem, sh});
+    *out = sh;
+    return RAD_OK;
+}
+
 template <typename T>
 int upload(const Scene<T>& s, const Octree<T>& o, const rad_options& opt, int device, DevImpl<T>& d) {
     d.device = device;
@@ -507,27 +583,85 @@ int upload(const Scene<T>& s, const Octree<T>& o, const rad_options& opt, int de
     const int n = s.trinum;
     if (n < 0) return fail(RAD_ERR_ARG, "negative slot count");
     if (!thresholds_consistent(o)) return fail(RAD_ERR_ARG, "octree cell thresholds do not match its dimensions");
-    // The kernels' records are packed on the host into this thread's pinned
-    // staging (reused between handles, so no page faults) and copied from
-    // there: the six per-slot arrays as one block, then the walk's triangle
-    // records and the octree's compact tables, which are expanded on the
-    // device in this thread's preparation scratch.  Only the records the
-    // solver keeps are allocated for the handle.
-    int n_tri = 0;
-    for (int32_t id : o.entry_tri) n_tri = std::max(n_tri, id + 1);
+    const int n_tri = max_entry_tri(o.entry_tri, opt.jobs);
     if (n_tri > n) return fail(RAD_ERR_ARG, "octree names a triangle beyond the scene");
     const long long n_cell = (long long)o.cell_leaf.size(), n_ent = (long long)o.entry_tri.size();
     const size_t n_rec = (size_t)n * 10;            // vtx 3, acc 3, nrm, ctr, frgb, db per slot
     const size_t n_trec = (size_t)n_tri * 5;
+
+    // the kernels' launch shapes: k_shoot is persistent, as many CTAs as fit at once
+    d.n_thr = (int)o.thr.size();
+    const int n_groups = (n + kSlotsPerWarp - 1) / kSlotsPerWarp;
+    {
+        ShootShape sh;
+        int rc0;
+        if ((rc0 = shoot_shape<T>(device, d.shoot_smem(), &sh))) return rc0;
+        const int want = (n_groups + kShootThreads / 32 - 1) / (kShootThreads / 32);
+        d.n_cta1 = std::max(1, std::min(want, std::max(1, sh.sms * sh.per1)));
+        d.n_cta_nf = std::max(1, std::min(want, std::max(1, sh.sms * sh.per_nf)));
+        d.n_cta2 = std::max(1, std::min(want, std::max(1, sh.sms * sh.per2)));
+        // the throughput form once there are over 4 groups per resident warp
+        const long long warps2 = (long long)sh.sms * std::max(sh.per2, 1) * (kShootThreads / 32);
+        d.layout = (std::is_same<T, float>::value && d.P == 1 && n_groups > 4 * warps2) ? 2 : 1;
+        d.n_cta = d.n_cta_of(d.layout);
+    }
+
+    // Every array the handle keeps, carved from one device allocation.
+    Q4<T>* d_rec;
+    Q4<T>* d_ent;
+    CellRec<T>* d_cell;
+    T* d_thr;
+    int *d_heavy, *d_stamp, *d_early, *d_estamp;
+    DevBlock blk;
+    blk.add(&d_rec, n_rec);
+    blk.add(&d_thr, o.thr.size());
+    blk.add(&d_cell, (size_t)n_cell);
+    blk.add(&d_ent, (size_t)n_ent * 5);
+    blk.add(&d.d_shooters, (size_t)d.P);
+    blk.add(&d.d_state, 1);
+    blk.add(&d.d_part, (size_t)std::max({d.n_cta1, d.n_cta2, d.n_cta_nf}));
+    blk.add(&d_heavy, 2 * (size_t)n_groups);
+    blk.add(&d_stamp, (size_t)n_groups);
+    blk.add(&d.d_unshot, (size_t)kUnshotCtas + 1);
+    blk.add(&d_early, 2 * (size_t)n_groups);
+    blk.add(&d_estamp, (size_t)n_groups);
+    d.trace_cap = 1 << 16;
+    blk.add(&d.d_trace, (size_t)d.trace_cap);
+    int rc;
+    if ((rc = d.alloc_block(blk))) return rc;
+    Q4<T>* d_vtx = d_rec;
+    Q4<T>* d_acc = d_vtx + (size_t)n * 3;
+    Q4<T>* d_nrm = d_acc + (size_t)n * 3;
+    Q4<T>* d_ctr = d_nrm + n;
+    Q4<T>* d_frgb = d_ctr + n;
+    Q4<T>* d_db = d_frgb + n;
+
+    // The records are packed on the host into this thread's pinned staging
+    // (reused between handles, so no page faults) on the host pool's threads,
+    // and copied from there in three pieces: the six per-slot arrays into the
+    // handle's block; the walk's triangle records with the octree's compact
+    // tables, laid out as in the staging, into this thread's preparation
+    // scratch, where k_expand_cells and k_gather_entries build the cell table
+    // and the list entries the handle keeps; and the cell thresholds.
+    HostLayout lay;
+    const size_t o_rec = lay.add(n_rec * sizeof(Q4<T>));
+    const size_t o_trec = lay.add(n_trec * sizeof(Q4<T>));
+    const size_t o_cleaf = lay.add(o.cell_leaf.size() * 4);
+    const size_t o_lbox = lay.add(o.leaf_box.size() * sizeof(T));
+    const size_t o_lrange = lay.add(o.leaf_range.size() * 4);
+    const size_t o_etri = lay.add(o.entry_tri.size() * 4);
+    const size_t o_tab_end = lay.size;
+    const size_t o_thr = lay.add(o.thr.size() * sizeof(T));
     void* stage_p = nullptr;
-    CU(pinned_stage().get((n_rec + n_trec) * sizeof(Q4<T>), &stage_p));
-    Q4<T>* h_vtx = static_cast<Q4<T>*>(stage_p);
+    CU(pinned_stage().get(lay.size, &stage_p));
+    char* stage = static_cast<char*>(stage_p);
+    Q4<T>* h_vtx = reinterpret_cast<Q4<T>*>(stage + o_rec);
     Q4<T>* h_acc = h_vtx + (size_t)n * 3;
     Q4<T>* h_nrm = h_acc + (size_t)n * 3;
     Q4<T>* h_ctr = h_nrm + n;
     Q4<T>* h_frgb = h_ctr + n;
     Q4<T>* h_db = h_frgb + n;
-    Q4<T>* h_trec = h_db + n;
+    Q4<T>* h_trec = reinterpret_cast<Q4<T>*>(stage + o_trec);
     // slots [a, b): their records, and the walk's triangle records of the
     // triangles among them that a list names (five per triangle)
     auto pack = [&](int a, int b) {
@@ -550,62 +684,35 @@ int upload(const Scene<T>& s, const Octree<T>& o, const rad_options& opt, int de
             }
         }
     };
-    // a memory-bound pass: large scenes split it over the -jobs host threads
-    const int jobs = n >= 16384 ? std::max(1, std::min({opt.jobs, 16, n / 8192})) : 1;
-    if (jobs <= 1) {
-        pack(0, n);
-    } else {
-        auto lo = [&](int j) { return (int)((long long)n * j / jobs); };
-        std::vector<std::thread> pool;
-        int started = 1;
-        try {
-            for (; started < jobs; started++) pool.emplace_back(pack, lo(started), lo(started + 1));
-        } catch (...) {   // chunks whose thread could not start are packed here
-        }
-        for (int j = started; j < jobs; j++) pack(lo(j), lo(j + 1));
-        pack(0, lo(1));
-        for (auto& th : pool) th.join();
-    }
-    Q4<T>* d_rec;
-    Q4<T>* d_ent;
-    CellRec<T>* d_cell;
-    T* d_thr;
-    int rc;
-    if ((rc = d.alloc(&d_rec, n_rec)) || (rc = d.alloc(&d_thr, o.thr.size())) || (rc = d.alloc(&d_cell, (size_t)n_cell)) ||
-        (rc = d.alloc(&d_ent, (size_t)n_ent * 5)))
-        return rc;
-    Q4<T>* d_vtx = d_rec;
-    Q4<T>* d_acc = d_vtx + (size_t)n * 3;
-    Q4<T>* d_nrm = d_acc + (size_t)n * 3;
-    Q4<T>* d_ctr = d_nrm + n;
-    Q4<T>* d_frgb = d_ctr + n;
-    Q4<T>* d_db = d_frgb + n;
+    // memory-bound passes: large scenes split them over the host pool
+    const int jobs = pack_jobs(n, opt.jobs);
+    split_range(n, jobs, pack);
+    copy_segments({{stage + o_cleaf, o.cell_leaf.data(), o.cell_leaf.size() * 4},
+                   {stage + o_lbox, o.leaf_box.data(), o.leaf_box.size() * sizeof(T)},
+                   {stage + o_lrange, o.leaf_range.data(), o.leaf_range.size() * 4},
+                   {stage + o_etri, o.entry_tri.data(), o.entry_tri.size() * 4},
+                   {stage + o_thr, o.thr.data(), o.thr.size() * sizeof(T)}},
+                  jobs);
     auto h2d = [&](void* dst, const void* src, size_t bytes) -> int {
         if (bytes) CU(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, d.stream));
         d.h2d_bytes += (long long)bytes;
         return RAD_OK;
     };
     PrepWorkspace& ws = prep_workspace(device);
-    void *t_trec, *t_cleaf, *t_lbox, *t_lrange, *t_etri;
-    CU(ws.buffer(8, std::max<size_t>(n_trec * sizeof(Q4<T>), 16), &t_trec));
-    CU(ws.buffer(9, std::max<size_t>(o.cell_leaf.size() * 4, 16), &t_cleaf));
-    CU(ws.buffer(10, std::max<size_t>(o.leaf_box.size() * sizeof(T), 16), &t_lbox));
-    CU(ws.buffer(11, std::max<size_t>(o.leaf_range.size() * 4, 16), &t_lrange));
-    CU(ws.buffer(12, std::max<size_t>(o.entry_tri.size() * 4, 16), &t_etri));
-    if ((rc = h2d(d_rec, h_vtx, n_rec * sizeof(Q4<T>))) || (rc = h2d(t_trec, h_trec, n_trec * sizeof(Q4<T>))) ||
-        (rc = h2d(d_thr, o.thr.data(), o.thr.size() * sizeof(T))) ||
-        (rc = h2d(t_cleaf, o.cell_leaf.data(), o.cell_leaf.size() * 4)) ||
-        (rc = h2d(t_lbox, o.leaf_box.data(), o.leaf_box.size() * sizeof(T))) ||
-        (rc = h2d(t_lrange, o.leaf_range.data(), o.leaf_range.size() * 4)) ||
-        (rc = h2d(t_etri, o.entry_tri.data(), o.entry_tri.size() * 4)))
+    void* scratch;
+    CU(ws.buffer(8, std::max<size_t>(o_tab_end - o_trec, 16), &scratch));
+    auto tab = [&](size_t off) { return static_cast<char*>(scratch) + (off - o_trec); };   // staging offsets
+    if ((rc = h2d(d_rec, stage + o_rec, n_rec * sizeof(Q4<T>))) ||
+        (rc = h2d(tab(o_trec), stage + o_trec, o_tab_end - o_trec)) ||
+        (rc = h2d(d_thr, stage + o_thr, o.thr.size() * sizeof(T))))
         return rc;
     if (n_cell > 0)
         k_expand_cells<T><<<(int)std::min<long long>((n_cell + 255) / 256, 4096), 256, 0, d.stream>>>(
-            static_cast<const int32_t*>(t_cleaf), static_cast<const T*>(t_lbox), static_cast<const int32_t*>(t_lrange),
-            n_cell, d_cell);
+            reinterpret_cast<const int32_t*>(tab(o_cleaf)), reinterpret_cast<const T*>(tab(o_lbox)),
+            reinterpret_cast<const int32_t*>(tab(o_lrange)), n_cell, d_cell);
     if (n_ent > 0)
         k_gather_entries<T><<<(int)std::min<long long>((n_ent * 5 + 255) / 256, 4096), 256, 0, d.stream>>>(
-            static_cast<const int32_t*>(t_etri), static_cast<const Q4<T>*>(t_trec), n_ent, d_ent);
+            reinterpret_cast<const int32_t*>(tab(o_etri)), reinterpret_cast<const Q4<T>*>(tab(o_trec)), n_ent, d_ent);
     CU(cudaGetLastError());
     d.S = Slots<T>{n, d_vtx, d_nrm, d_ctr, d_frgb, d_acc, d_db};
     Grid<T> G = grid_params(o, opt.walk_cap);
@@ -614,48 +721,9 @@ int upload(const Scene<T>& s, const Octree<T>& o, const rad_options& opt, int de
     G.entry = d_ent;
     d.G = G;
 
-    // per-step state; k_shoot is persistent: as many CTAs as fit at once
-    d.n_thr = (int)o.thr.size();
-    if (d.shoot_smem() > 48 * 1024) {
-        CU(cudaFuncSetAttribute(k_shoot<T, false, false, 3, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)d.shoot_smem()));
-        CU(cudaFuncSetAttribute(k_shoot<T, true, false, 3, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)d.shoot_smem()));
-        CU(cudaFuncSetAttribute(k_shoot<T, false, true, kForm1MinBlocks<T>, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)d.shoot_smem()));
-        CU(cudaFuncSetAttribute(k_shoot<T, true, true, 3, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)d.shoot_smem()));
-        if constexpr (std::is_same<T, float>::value)
-            CU(cudaFuncSetAttribute(k_shoot<T, false, true, 4, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)d.shoot_smem()));
-    }
-    const int n_groups = (n + kSlotsPerWarp - 1) / kSlotsPerWarp;
-    {
-        int sms = 0, per1 = 0, per2 = 0;
-        CU(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
-        CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per1, k_shoot<T, false, true, kForm1MinBlocks<T>, 4>, kShootThreads, d.shoot_smem()));
-        int per_nf = 0;
-        CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_nf, k_shoot<T, false, false, 3, 4>, kShootThreads, d.shoot_smem()));
-        if constexpr (std::is_same<T, float>::value)
-            CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per2, k_shoot<T, false, true, 4, 1>, kShootThreads,
-                                                             d.shoot_smem()));
-        else
-            per2 = per1;
-        const int want = (n_groups + kShootThreads / 32 - 1) / (kShootThreads / 32);
-        d.n_cta1 = std::max(1, std::min(want, std::max(1, sms * per1)));
-        d.n_cta_nf = std::max(1, std::min(want, std::max(1, sms * per_nf)));
-        d.n_cta2 = std::max(1, std::min(want, std::max(1, sms * per2)));
-        // the throughput form once there are over 4 groups per resident warp
-        const long long warps2 = (long long)sms * std::max(per2, 1) * (kShootThreads / 32);
-        d.layout = (std::is_same<T, float>::value && d.P == 1 && n_groups > 4 * warps2) ? 2 : 1;
-        d.n_cta = d.n_cta_of(d.layout);
-    }
-    int *d_heavy, *d_stamp, *d_early, *d_estamp;
-    if ((rc = d.alloc(&d.d_shooters, (size_t)d.P)) || (rc = d.alloc(&d.d_state, 1)) ||
-        (rc = d.alloc(&d.d_part, (size_t)std::max({d.n_cta1, d.n_cta2, d.n_cta_nf}))) || (rc = d.alloc(&d_heavy, 2 * (size_t)n_groups)) ||
-        (rc = d.alloc(&d_stamp, (size_t)n_groups)) || (rc = d.alloc(&d.d_unshot, (size_t)kUnshotCtas + 1)) ||
-        (rc = d.alloc(&d_early, 2 * (size_t)n_groups)) || (rc = d.alloc(&d_estamp, (size_t)n_groups)))
-        return rc;
+    // per-step state
     CU(cudaMemsetAsync(d_stamp, 0xff, (size_t)n_groups * sizeof(int), d.stream));
     CU(cudaMemsetAsync(d_estamp, 0xff, (size_t)n_groups * sizeof(int), d.stream));
-    d.trace_cap = 1 << 16;
-    CU(cudaMalloc(&d.d_trace, (size_t)d.trace_cap * 4));
     State st{};
     st.step_limit = 0;
     st.trace = d.d_trace;
@@ -680,7 +748,6 @@ int upload(const Scene<T>& s, const Octree<T>& o, const rad_options& opt, int de
     // initial selection keys: a step with no shooter only reduces the keys
     launch_shoot(d, d.stream);
     CU(cudaGetLastError());
-    CU(cudaStreamSynchronize(d.stream));
     CU(cudaMemcpyAsync(&st, d.d_state, sizeof st, cudaMemcpyDeviceToHost, d.stream));
     CU(cudaStreamSynchronize(d.stream));
     d.host = st;
@@ -715,9 +782,19 @@ int launch_step(DevImpl<T>& d, cudaStream_t s) {
     return RAD_OK;
 }
 
+// The graph of a chunk of `steps` steps, built the second time a chunk of
+// that shape runs; null the first time, when the caller launches the steps
+// one by one: a step's kernel outlasts its launch, so the launches overlap the
+// device's work, while capturing and instantiating a graph would delay it.
 template <typename T>
 int graph_for(DevImpl<T>& d, int steps, cudaGraphExec_t* out) {
     cudaGraphExec_t& slot = d.graphs[d.layout][d.counting ? 1 : 0][steps];
+    bool& seen = d.graph_seen[d.layout][d.counting ? 1 : 0][steps];
+    if (!slot && !seen) {
+        seen = true;
+        *out = nullptr;
+        return RAD_OK;
+    }
     if (!slot) {
         cudaGraph_t g;
         CU(cudaStreamBeginCapture(d.stream, cudaStreamCaptureModeThreadLocal));
@@ -743,8 +820,9 @@ int grow_trace(DevImpl<T>& d, long long need) {
     CU(cudaMalloc(&nt, (size_t)cap * 4));
     CU(cudaMemcpyAsync(nt, d.d_trace, (size_t)d.trace_cap * 4, cudaMemcpyDeviceToDevice, d.stream));
     CU(cudaStreamSynchronize(d.stream));
-    cudaFree(d.d_trace);
+    if (d.trace_own) cudaFree(d.d_trace);
     d.d_trace = nt;
+    d.trace_own = true;
     d.trace_cap = cap;
     CU(cudaMemcpyAsync(&d.d_state->trace, &nt, sizeof(int*), cudaMemcpyHostToDevice, d.stream));
     CU(cudaMemcpyAsync(&d.d_state->trace_cap, &cap, sizeof(long long), cudaMemcpyHostToDevice, d.stream));
@@ -791,7 +869,12 @@ int run(DevImpl<T>& d, long long max_steps, long long* done_steps, int* converge
             cudaGraphExec_t g;
             if ((rc = graph_for(d, chunk, &g))) return rc;
             if (mode) CU(cudaEventRecord(d.ev[0], d.stream));
-            CU(cudaGraphLaunch(g, d.stream));
+            if (g) {
+                CU(cudaGraphLaunch(g, d.stream));
+            } else {
+                for (int k = 0; k < chunk; k++)
+                    if ((rc = launch_step(d, d.stream))) return rc;
+            }
             if (mode) CU(cudaEventRecord(d.ev[2], d.stream));
         }
         CU(cudaMemcpyAsync(&d.host, d.d_state, sizeof(State), cudaMemcpyDeviceToHost, d.stream));
@@ -830,13 +913,15 @@ int download(DevImpl<T>& d, Scene<T>& s) {
         CU(cudaMemcpyAsync(db, d.S.deltaB, (size_t)n * sizeof(Q4<T>), cudaMemcpyDeviceToHost, d.stream));
     }
     CU(cudaStreamSynchronize(d.stream));
-    for (int i = 0; i < n; i++) {
-        Slot<T>& t = s.slots[i];
-        for (int v = 0; v < 3; v++) {
-            t.accB[v][0] = acc[i * 3 + v].x; t.accB[v][1] = acc[i * 3 + v].y; t.accB[v][2] = acc[i * 3 + v].z;
+    split_range(n, pack_jobs(n, s.opt.jobs), [&](int a, int b) {
+        for (int i = a; i < b; i++) {
+            Slot<T>& t = s.slots[i];
+            for (int v = 0; v < 3; v++) {
+                t.accB[v][0] = acc[i * 3 + v].x; t.accB[v][1] = acc[i * 3 + v].y; t.accB[v][2] = acc[i * 3 + v].z;
+            }
+            t.deltaB[0] = db[i].x; t.deltaB[1] = db[i].y; t.deltaB[2] = db[i].z;
         }
-        t.deltaB[0] = db[i].x; t.deltaB[1] = db[i].y; t.deltaB[2] = db[i].z;
-    }
+    });
     return RAD_OK;
 }
 
@@ -1055,7 +1140,7 @@ int rad_dev_stats(const rad_dev* h, rad_stats* st) {
         st->walk_loops = (int64_t)d.host.loops;
         st->converged = d.host.done;
         st->n_slots = d.S.n;
-        st->device_bytes = (int64_t)(d.bytes + d.trace_cap * 4);
+        st->device_bytes = (int64_t)(d.bytes + (d.trace_own ? d.trace_cap * 4 : 0));
         st->h2d_bytes = (int64_t)d.h2d_bytes;
         using TT = typename std::remove_reference<decltype(d)>::type::Real;
         k_unshot<TT><<<kUnshotCtas, kUnshotThreads, 0, d.stream>>>(d.S, d.d_unshot);
