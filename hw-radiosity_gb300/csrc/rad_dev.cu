@@ -1076,6 +1076,12 @@ int rad_dev_run(rad_dev* h, int64_t max_steps, int64_t* steps_done, int32_t* con
     return rc;
 }
 
+int rad_dev_stream(const rad_dev* h, void** stream) {
+    if (!h || !stream) return fail(RAD_ERR_ARG, "rad_dev_stream: null argument");
+    *stream = h->d32 ? (void*)h->d32->stream : (void*)h->d64->stream;
+    return RAD_OK;
+}
+
 int rad_dev_run_timed(rad_dev* h, int64_t max_steps, int64_t* steps_done, int32_t* converged, double* device_ms) {
     if (!h) return fail(RAD_ERR_ARG, "rad_dev_run_timed: null handle");
     long long sd = 0;

@@ -24,7 +24,7 @@ EXPORTS = [
     "rad_scene_load", "rad_scene_from_arrays", "rad_scene_init", "rad_scene_init_device", "rad_scene_prepartition",
     "rad_scene_view_get", "rad_scene_write_fin", "rad_scene_log", "rad_scene_free",
     "rad_octree_build", "rad_octree_build_device", "rad_octree_tables", "rad_octree_info", "rad_octree_cell_coords", "rad_octree_free",
-    "rad_dev_create", "rad_dev_run", "rad_dev_run_timed", "rad_dev_run_profiled", "rad_dev_download", "rad_dev_trace", "rad_dev_stats",
+    "rad_dev_create", "rad_dev_run", "rad_dev_stream", "rad_dev_run_timed", "rad_dev_run_profiled", "rad_dev_download", "rad_dev_trace", "rad_dev_stats",
     "rad_dev_set_counting", "rad_dev_set_schedule", "rad_dev_set_layout", "rad_dev_layout", "rad_dev_autotune", "rad_dev_ray_hit", "rad_dev_form_factors", "rad_dev_form_factors_noalloc",
     "rad_dev_destroy",
     "rad_batch_create", "rad_batch_run", "rad_batch_run_timed", "rad_batch_scene_stats", "rad_batch_download",
@@ -103,6 +103,7 @@ def load(path: Optional[str] = None) -> C.CDLL:
         "rad_octree_free": (None, [vp]),
         "rad_dev_create": (C.c_int, [vp, vp, P(Options), i32, P(vp)]),
         "rad_dev_run": (C.c_int, [vp, i64, P(i64), P(i32)]),
+        "rad_dev_stream": (C.c_int, [vp, P(vp)]),
         "rad_dev_run_timed": (C.c_int, [vp, i64, P(i64), P(i32), P(C.c_double)]),
         "rad_dev_run_profiled": (C.c_int, [vp, i64, P(i64), P(i32), P(C.c_double), P(C.c_double)]),
         "rad_dev_download": (C.c_int, [vp, vp]),
@@ -320,6 +321,12 @@ class Device:
         cv = C.c_int32()
         rc = _check(load().rad_dev_run(self.h, max_steps, C.byref(sd), C.byref(cv)), allow=(RAD_ERR_WALK,))
         return sd.value, bool(cv.value), rc
+
+    def stream(self) -> int:
+        """The handle's CUDA stream (a cudaStream_t, as an integer)."""
+        p = C.c_void_p()
+        _check(load().rad_dev_stream(self.h, C.byref(p)))
+        return p.value or 0
 
     def run_timed(self, max_steps: int):
         """(steps, converged, device milliseconds) for up to max_steps steps."""

@@ -176,6 +176,11 @@ int rad_dev_create(const rad_scene* s, const rad_octree* t, const rad_options* o
  * when a selection finds no candidate (*converged = 1).  Steps are issued in
  * CUDA-graph chunks; the host synchronises once per chunk. */
 int rad_dev_run(rad_dev* d, int64_t max_steps, int64_t* steps_done, int32_t* converged);
+/* The CUDA stream (a cudaStream_t) the handle's steps, downloads and queries
+ * run on (no reference counterpart).  Work the caller enqueues there runs
+ * before the steps of its next rad_dev_run* call, without a host round trip:
+ * a timing loop that clears L2 between steps enqueues the clearing there. */
+int rad_dev_stream(const rad_dev* d, void** stream);
 /* rad_dev_run, also reporting the device time of the executed steps in
  * milliseconds (CUDA events on the solver's stream around the graph
  * launches; host synchronisation is outside the measured interval). */
