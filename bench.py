@@ -367,27 +367,45 @@ def measure_adaptive(capi, steps, device, with_reference=True):
     """The adaptive split variant (ADAPT + ROLLBACK build of the reference) on
     a 100x100x100 room with 4 boxes that splits from 960 triangles toward the
     40,000 cap: wall-clock steps/s of the GPU + host solver, next to the
-    reference's own adaptive build (serial by construction) on the same steps."""
+    reference's own adaptive build (serial by construction) on the same steps.
+    Both speculation modes run; their results must be bit-identical."""
+    import numpy as np
     from hwrad import scenes as S
     sc_gen = S.room_with_boxes(8, 4, 1, seed=5, size=100.0)
     argv = sc_gen.argv({"-triangle": "40000", "-converge": "5"})
     tmp = tempfile.mkdtemp(prefix="radadapt_")
     tri = sc_gen.write(os.path.join(tmp, "adapt.tri"))
     o = capi.options_from_argv(argv)
-    sc = capi.Scene.load(tri, o)
-    tree = capi.Octree(sc, _nproc())
-    sc.init()
-    ad = capi.Adaptive(sc, tree, o, device)
-    t0 = time.perf_counter()
-    n, conv, _ = ad.run(steps)
-    dt = time.perf_counter() - t0
-    st = ad.stats()
+
+    def one(wait):
+        sc = capi.Scene.load(tri, o)
+        tree = capi.Octree(sc, _nproc())
+        sc.init()
+        ad = capi.Adaptive(sc, tree, o, device)
+        ad.set_speculation(wait)
+        t0 = time.perf_counter()
+        n, conv, _ = ad.run(steps)
+        dt = time.perf_counter() - t0
+        st = ad.stats()
+        trace = ad.trace()
+        ad.close()
+        v = sc.view()
+        res = {"steps": n, "steps_per_s": n / dt if dt > 0 else None, "host_form_factors": st["host_points"],
+               "device_sample_points": st["device_points"], "speculations": st["speculations"]}
+        return res, st, (trace, v["accB"].copy(), v["deltaB"].copy(), v["parent"].copy())
+
+    race, st, r_state = one(False)
+    wait, _, w_state = one(True)
+    same = all(np.array_equal(a, b) for a, b in zip(r_state, w_state))
     out = {"workload": "room 100^3, 4 boxes, 960 triangles splitting toward the 40,000 cap, -converge 5",
-           "steps": n, "slots_end": st["n_slots"], "steps_per_s": n / dt if dt > 0 else None,
-           "rays": st["rays"], "splits": st["splits"], "host_form_factors": st["host_points"],
-           "sample_points": st["samples"], "device_sample_points": st["device_points"],
-           "speculations": st["speculations"], "split_candidates": st["split_candidates"]}
-    ad.close()
+           "steps": race["steps"], "slots_end": st["n_slots"], "steps_per_s": race["steps_per_s"],
+           "rays": st["rays"], "splits": st["splits"], "host_form_factors": race["host_form_factors"],
+           "sample_points": st["samples"], "device_sample_points": race["device_sample_points"],
+           "speculations": race["speculations"], "split_candidates": st["split_candidates"],
+           "speculation": "raced by the host (default)",
+           "waiting_speculation": {k: wait[k] for k in ("steps_per_s", "host_form_factors",
+                                                        "device_sample_points", "speculations")},
+           "modes_bit_identical": bool(same)}
     if with_reference:
         sys.path.insert(0, os.path.join(REPO, "oracle"))
         import runner

@@ -377,6 +377,13 @@ struct AdaptImpl {
     unsigned* dm_live = nullptr;
     unsigned sp_gen = 0;
     cudaEvent_t copies_done = nullptr;    // the step's test results are on the host
+    cudaEvent_t sp_done = nullptr;        // recorded after each speculation
+    // 0: the host races the speculation (takes the points already written,
+    //    evaluates the others itself, re-speculates as soon as a receiver
+    //    moves the stream); 1: the host waits for each new speculation to
+    //    finish, started only when the next sampling receiver needs it
+    int spec_wait_mode = 0;
+    bool sp_finished = false;             // the current speculation has been waited for
     long long dev_samples = 0, spec_launches = 0, split_candidates = 0;
     std::vector<void*> pinned;
 
@@ -384,6 +391,7 @@ struct AdaptImpl {
         if (h_live) __atomic_store_n(h_live, sp_gen + 1, __ATOMIC_RELEASE);   // stop a running speculation
         if (stream) cudaStreamSynchronize(stream);
         if (copies_done) cudaEventDestroy(copies_done);
+        if (sp_done) cudaEventDestroy(sp_done);
         for (void* p : allocs) cudaFree(p);
         for (void* p : pinned) cudaFreeHost(p);
         if (stream) cudaStreamDestroy(stream);
@@ -498,6 +506,7 @@ int adapt_create(Scene<T>& s, const Octree<T>& o, const rad_options& opt, int de
     std::memset(a.h_stag, 0, (size_t)a.task_cap * sizeof(unsigned));
     *a.h_live = 0;
     CU(cudaEventCreateWithFlags(&a.copies_done, cudaEventDisableTiming));
+    CU(cudaEventCreateWithFlags(&a.sp_done, cudaEventDisableTiming));
     a.ff.assign((size_t)a.cap * 4, (T)0);
     a.mod_step.assign((size_t)a.cap, 0);
     a.dirty.assign((size_t)a.cap, 0);
@@ -536,6 +545,7 @@ int spec_cancel(AdaptImpl<T>& a) {
     a.sp_gen++;
     __atomic_store_n(a.h_live, a.sp_gen, __ATOMIC_RELEASE);
     a.sp_start = a.sp_end = a.sp_base = 0;
+    a.sp_finished = false;
     return RAD_OK;
 }
 
@@ -562,6 +572,7 @@ int spec_enqueue(AdaptImpl<T>& a, const Slots<T>& S, int n0, long long start, lo
                                                      a.ring_len, a.dm_sff, a.dm_scode, a.dm_stag, a.dm_live,
                                                      a.sp_gen);
     CU(cudaGetLastError());
+    CU(cudaEventRecord(a.sp_done, a.stream));
     return RAD_OK;
 }
 
@@ -626,6 +637,13 @@ struct StepCtx {
             if (int rc = spec_enqueue(a, S, n0, t0, cur, a.h_toff[n0])) { err = rc; return -1; }
             if (!covered(t0, n, cur)) return -1;
         }
+        if (a.spec_wait_mode && !a.sp_finished) {       // the whole speculation, once
+            if (cudaEventSynchronize(a.sp_done) != cudaSuccess) {
+                err = fail(RAD_ERR_CUDA, "sample-point kernel failed");
+                return -1;
+            }
+            a.sp_finished = true;
+        }
         return t0;
     }
 
@@ -635,7 +653,7 @@ struct StepCtx {
     // would), start the speculation from there now, so that it runs while the
     // host gets to that receiver.
     void respeculate_after(int d) {
-        if (d + 1 >= n0 || a.rng.pos % 3 != 0) return;
+        if (a.spec_wait_mode || d + 1 >= n0 || a.rng.pos % 3 != 0) return;
         const long long t = a.h_toff[d + 1];
         if (t >= a.h_toff[n0] || covered(t, 1, a.rng.pos / 3)) return;
         if (int rc = spec_enqueue(a, S, n0, t, a.rng.pos / 3, a.h_toff[n0])) err = rc;
@@ -886,6 +904,14 @@ int rad_adapt_stats(const rad_adapt* h, rad_stats* st, int64_t* host_points, int
         return RAD_OK;
     };
     return h->a32 ? go(*h->a32) : go(*h->a64);
+}
+
+int rad_adapt_set_speculation(rad_adapt* h, int32_t wait) {
+    if (!h) return fail(RAD_ERR_ARG, "rad_adapt_set_speculation: null handle");
+    if (wait != 0 && wait != 1) return fail(RAD_ERR_ARG, "rad_adapt_set_speculation: wait is 0 or 1");
+    if (h->a32) h->a32->spec_wait_mode = wait;
+    else h->a64->spec_wait_mode = wait;
+    return RAD_OK;
 }
 
 int rad_adapt_device_stats(const rad_adapt* h, int64_t* device_points, int64_t* speculations,

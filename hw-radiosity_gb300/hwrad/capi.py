@@ -29,7 +29,7 @@ EXPORTS = [
     "rad_dev_destroy",
     "rad_batch_create", "rad_batch_run", "rad_batch_run_timed", "rad_batch_scene_stats", "rad_batch_download",
     "rad_batch_trace", "rad_batch_stats", "rad_batch_set_counting", "rad_batch_destroy",
-    "rad_adapt_create", "rad_adapt_run", "rad_adapt_trace", "rad_adapt_stats", "rad_adapt_destroy",
+    "rad_adapt_create", "rad_adapt_run", "rad_adapt_trace", "rad_adapt_stats", "rad_adapt_set_speculation", "rad_adapt_destroy",
     "rad_render_options_default", "rad_render_fin", "rad_render_scene",
 ]
 
@@ -135,6 +135,7 @@ def load(path: Optional[str] = None) -> C.CDLL:
         "rad_adapt_run": (C.c_int, [vp, i64, P(i64), P(i32)]),
         "rad_adapt_trace": (C.c_int, [vp, vp, i64, P(i64)]),
         "rad_adapt_stats": (C.c_int, [vp, P(Stats), P(i64), P(i64), P(i64)]),
+        "rad_adapt_set_speculation": (C.c_int, [vp, i32]),
         "rad_adapt_destroy": (None, [vp]),
         "rad_render_options_default": (None, [P(RenderOptions)]),
         "rad_render_fin": (C.c_int, [C.c_char_p, P(RenderOptions), i32, vp]),
@@ -503,6 +504,10 @@ class Adaptive:
         sd, cv = C.c_int64(), C.c_int32()
         rc = _check(load().rad_adapt_run(self.h, max_steps, C.byref(sd), C.byref(cv)), allow=(RAD_ERR_WALK,))
         return sd.value, bool(cv.value), rc
+
+    def set_speculation(self, wait: bool):
+        """False: race the device's sample points (default); True: wait for each speculation."""
+        _check(load().rad_adapt_set_speculation(self.h, 1 if wait else 0))
 
     def trace(self) -> np.ndarray:
         n = C.c_int64()

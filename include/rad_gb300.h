@@ -331,6 +331,15 @@ int rad_adapt_trace(const rad_adapt* a, int32_t* out, int64_t cap, int64_t* n);
 /* host_points: form factors evaluated on the host (sample points, receivers
  * rewritten earlier in their step); splits; rand() sample points drawn. */
 int rad_adapt_stats(const rad_adapt* a, rad_stats* st, int64_t* host_points, int64_t* splits, int64_t* samples);
+/* How the host takes the device's sample points (no reference counterpart;
+ * results do not depend on it).  wait = 0 (the default): when a receiver's
+ * sample loop moves the rand() stream off the speculation, a new speculation
+ * starts at once from the next receiver, and the host takes each point the
+ * device has already written and evaluates the others itself (fewer stalls,
+ * more host form factors).  wait = 1: a new speculation starts when the next
+ * sampling receiver needs it, and the host waits for it to finish (more
+ * stalls, fewer host form factors). */
+int rad_adapt_set_speculation(rad_adapt* a, int32_t wait);
 /* The device's share (no reference counterpart): sample points whose form
  * factor came from the device's speculation, speculation launches, and
  * receivers whose delta-FF test failed at the start of their step (summed

@@ -53,14 +53,15 @@ def test_adaptive_matches_reference_fixture(built, workdir, name):
     assert st["splits"] > 0 and st["rays"] > 0
 
 
-def test_adaptive_device_sample_points_bench_room(built, workdir):
+@pytest.mark.parametrize("wait", [False, True])
+def test_adaptive_device_sample_points_bench_room(built, workdir, wait):
     """The bench's adaptive workload (100^3 room, 4 boxes, splitting toward
-    40,000 slots), 30 steps: equal to the oracle bit for bit, with sample
-    points taken from the device's speculation.  The host takes the points
-    the device has written by the time it reads them and evaluates the rest,
-    so the device's share depends on how far the kernel runs ahead (about two
-    thirds on a GB300); the bound here only shows that the speculation is
-    used."""
+    40,000 slots), 30 steps, in both speculation modes: equal to the oracle
+    bit for bit, with sample points taken from the device's speculation.
+    Racing (the default), the host takes the points the device has written
+    by the time it reads them and evaluates the rest, so the device's share
+    depends on how far the kernel runs ahead (about two thirds on a GB300);
+    waiting, the host takes every point a speculation covers."""
     s = scenes.room_with_boxes(8, 4, 1, seed=5, size=100.0)
     tri = s.write(os.path.join(workdir, "ad_bench.tri"))
     argv = s.argv({"-triangle": "40000", "-converge": "5"})
@@ -69,6 +70,7 @@ def test_adaptive_device_sample_points_bench_room(built, workdir):
     tree = capi.Octree(sc, 4)
     sc.init()
     ad = capi.Adaptive(sc, tree, o)
+    ad.set_speculation(wait)
     for c in (1, 9, 20):
         ad.run(c)
     ref = runner.oracle(tri, argv, steps=30, adaptive=True)
@@ -78,7 +80,7 @@ def test_adaptive_device_sample_points_bench_room(built, workdir):
         assert same_bits(v[k], ref["dump"][k]), k
     st = ad.stats()
     assert st["samples"] > 1000
-    assert st["device_points"] > 0.2 * st["samples"]
+    assert st["device_points"] > (0.7 if wait else 0.2) * st["samples"]
     assert st["speculations"] >= 30
 
 
