@@ -181,50 +181,75 @@ k_shoot(Slots<T> S, Grid<T> G, Shooter<T>* shooters, State* st, Partial* __restr
     }
     warp_max(kk, ks);
     flush_counters<COUNT>(st, c, lane);
-    if (lane == 0) {
-        wkey[wid] = kk;
-        wslot[wid] = ks;
-    }
-    // The queue is empty: the CTA's warps meet (the early ones have nothing
-    // left to do) and thread 0 writes the CTA partial.
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        unsigned long long bk = 0;
-        int bs = -1;
-        for (int w = 0; w < kShootThreads / 32; w++)
-            if (part_less(bk, bs, wkey[w], wslot[w])) { bk = wkey[w]; bs = wslot[w]; }
-        part[blockIdx.x].key = bk;
-        part[blockIdx.x].slot = bs;
-        if (FUSED) {
+    constexpr bool kPacked = FUSED && std::is_same<T, float>::value;
+    if constexpr (kPacked) {
+        // One shooter in FP32: the (key, slot) maximum fits one 64-bit word
+        // (ties: the larger slot, as part_less orders them), so each CTA
+        // posts its own and the grid's last CTA reads the word, instead of
+        // reducing per-CTA partials.
+        if (lane == 0) wkey[wid] = ks >= 0 ? (kk << 32) | (unsigned long long)(unsigned)ks : 0ull;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            unsigned long long b = 0;
+            for (int w = 0; w < kShootThreads / 32; w++) b = wkey[w] > b ? wkey[w] : b;
+            if (b) atomicMax(&st->best, b);
             __threadfence();
             ndone = atomicAdd(&st->ctas_done, 1) == (int)gridDim.x - 1;
         }
-    }
-    if (!FUSED) return;
-    __syncthreads();
-    if (!ndone) return;
-    // the grid's last CTA: select the next step's shooter (listCanditate for
-    // one shooter), every thread reading a few CTA partials
-    __threadfence();
-    kk = 0;
-    ks = -1;
-    for (int q = threadIdx.x; q < (int)gridDim.x; q += blockDim.x) {
-        const unsigned long long qk = __ldcg(&part[q].key);
-        const int qs = __ldcg(&part[q].slot);
-        if (part_less(kk, ks, qk, qs)) { kk = qk; ks = qs; }
-    }
-    warp_max(kk, ks);
-    __syncthreads();          // wkey / wslot are reused
-    if (lane == 0) {
-        wkey[wid] = kk;
-        wslot[wid] = ks;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
+        __syncthreads();
+        if (!ndone || threadIdx.x != 0) return;
+        __threadfence();
+        const unsigned long long b = atomicExch(&st->best, 0ull);   // read and reset at L2
+        kk = b >> 32;
+        ks = b ? (int)(unsigned)(b & 0xffffffffull) : -1;
+    } else {
+        if (lane == 0) {
+            wkey[wid] = kk;
+            wslot[wid] = ks;
+        }
+        // The queue is empty: the CTA's warps meet (the early ones have nothing
+        // left to do) and thread 0 writes the CTA partial.
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            unsigned long long bk = 0;
+            int bs = -1;
+            for (int w = 0; w < kShootThreads / 32; w++)
+                if (part_less(bk, bs, wkey[w], wslot[w])) { bk = wkey[w]; bs = wslot[w]; }
+            part[blockIdx.x].key = bk;
+            part[blockIdx.x].slot = bs;
+            if (FUSED) {
+                __threadfence();
+                ndone = atomicAdd(&st->ctas_done, 1) == (int)gridDim.x - 1;
+            }
+        }
+        if (!FUSED) return;
+        __syncthreads();
+        if (!ndone) return;
+        // the grid's last CTA: select the next step's shooter (listCanditate for
+        // one shooter), every thread reading a few CTA partials
+        __threadfence();
+        kk = 0;
+        ks = -1;
+        for (int q = threadIdx.x; q < (int)gridDim.x; q += blockDim.x) {
+            const unsigned long long qk = __ldcg(&part[q].key);
+            const int qs = __ldcg(&part[q].slot);
+            if (part_less(kk, ks, qk, qs)) { kk = qk; ks = qs; }
+        }
+        warp_max(kk, ks);
+        __syncthreads();          // wkey / wslot are reused
+        if (lane == 0) {
+            wkey[wid] = kk;
+            wslot[wid] = ks;
+        }
+        __syncthreads();
+        if (threadIdx.x != 0) return;
         kk = 0;
         ks = -1;
         for (int w = 0; w < kShootThreads / 32; w++)
             if (part_less(kk, ks, wkey[w], wslot[w])) { kk = wkey[w]; ks = wslot[w]; }
+    }
+    // thread 0 of the grid's last CTA
+    {
         long long steps = st->steps + (nsh > 0 ? 1 : 0);    // the step just shot is complete
         if (!kk) {
             st->done = 1;
@@ -746,7 +771,7 @@ int upload(const Scene<T>& s, const Octree<T>& o, const rad_options& opt, int de
     CU(cudaMemsetAsync(d.d_shooters, 0, sizeof(Shooter<T>) * d.P, d.stream));
     CU(cudaMemsetAsync(d.d_part, 0, sizeof(Partial) * std::max({d.n_cta1, d.n_cta2, d.n_cta_nf}), d.stream));
     // initial selection keys: a step with no shooter only reduces the keys
-    launch_shoot(d, d.stream);
+    CU(launch_shoot(d, d.stream));
     CU(cudaGetLastError());
     CU(cudaMemcpyAsync(&st, d.d_state, sizeof st, cudaMemcpyDeviceToHost, d.stream));
     CU(cudaStreamSynchronize(d.stream));
@@ -755,29 +780,54 @@ int upload(const Scene<T>& s, const Octree<T>& o, const rad_options& opt, int de
 }
 
 // the shooting kernel of one step; with one shooter per step it also selects the next
+// the shooting kernel of one step; with one shooter per step it also selects the next
+// Launch with programmatic stream serialization: the grid may be scheduled
+// while the previous kernel on the stream is still finishing (k_shoot waits
+// for it with griddepcontrol.wait before reading anything).  In a graph chunk
+// the next step's CTAs then take the SMs its predecessor's tail leaves idle
+// and start the moment it completes.
+template <typename... KArgs, typename... Args>
+cudaError_t launch_overlapped(void (*kernel)(KArgs...), int grid, size_t smem, cudaStream_t s, Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3(kShootThreads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+
+// the shooting kernel of one step; with one shooter per step it also selects the next
 template <typename T>
-void launch_shoot(DevImpl<T>& d, cudaStream_t s) {
+cudaError_t launch_shoot(DevImpl<T>& d, cudaStream_t s) {
     const bool fused = d.P == 1;
+    const size_t sm = d.shoot_smem();
     // counting and several shooters per step use the tail-bound form at 3
     // CTAs per SM (they cannot re-read the deposit inputs); FP64 uses form 1
     if (d.counting && fused)
-        k_shoot<T, true, true, 3, 4><<<d.n_cta_nf, kShootThreads, d.shoot_smem(), s>>>(d.S, d.G, d.d_shooters, d.d_state, d.d_part, d.conv);
+        k_shoot<T, true, true, 3, 4><<<d.n_cta_nf, kShootThreads, sm, s>>>(d.S, d.G, d.d_shooters, d.d_state, d.d_part, d.conv);
     else if (d.counting)
-        k_shoot<T, true, false, 3, 4><<<d.n_cta_nf, kShootThreads, d.shoot_smem(), s>>>(d.S, d.G, d.d_shooters, d.d_state, d.d_part, d.conv);
+        k_shoot<T, true, false, 3, 4><<<d.n_cta_nf, kShootThreads, sm, s>>>(d.S, d.G, d.d_shooters, d.d_state, d.d_part, d.conv);
     else if (fused && d.layout == 2) {
         if constexpr (std::is_same<T, float>::value)
-            k_shoot<T, false, true, 4, 1><<<d.n_cta2, kShootThreads, d.shoot_smem(), s>>>(d.S, d.G, d.d_shooters, d.d_state,
-                                                                                       d.d_part, d.conv);
+            k_shoot<T, false, true, 4, 1><<<d.n_cta2, kShootThreads, sm, s>>>(d.S, d.G, d.d_shooters, d.d_state, d.d_part,
+                                                                           d.conv);
     } else if (fused)
-        k_shoot<T, false, true, kForm1MinBlocks<T>, 4><<<d.n_cta1, kShootThreads, d.shoot_smem(), s>>>(d.S, d.G, d.d_shooters, d.d_state, d.d_part, d.conv);
+        k_shoot<T, false, true, kForm1MinBlocks<T>, 4><<<d.n_cta1, kShootThreads, sm, s>>>(d.S, d.G, d.d_shooters, d.d_state,
+                                                                                          d.d_part, d.conv);
     else
-        k_shoot<T, false, false, 3, 4><<<d.n_cta_nf, kShootThreads, d.shoot_smem(), s>>>(d.S, d.G, d.d_shooters, d.d_state, d.d_part, d.conv);
+        k_shoot<T, false, false, 3, 4><<<d.n_cta_nf, kShootThreads, sm, s>>>(d.S, d.G, d.d_shooters, d.d_state, d.d_part, d.conv);
+    return cudaGetLastError();
 }
 
 template <typename T>
 int launch_step(DevImpl<T>& d, cudaStream_t s) {
     if (d.P > 1) k_setup<T><<<1, kSetupThreads, 0, s>>>(d.S, d.d_shooters, d.d_state, d.d_part, d.n_cta_nf, d.conv, d.P);
-    launch_shoot(d, s);
+    CU(launch_shoot(d, s));
     CU(cudaGetLastError());
     return RAD_OK;
 }
@@ -862,7 +912,7 @@ int run(DevImpl<T>& d, long long max_steps, long long* done_steps, int* converge
             CU(cudaEventRecord(d.ev[0], d.stream));
             if (d.P > 1) k_setup<T><<<1, kSetupThreads, 0, d.stream>>>(d.S, d.d_shooters, d.d_state, d.d_part, d.n_cta_nf, d.conv, d.P);
             CU(cudaEventRecord(d.ev[1], d.stream));
-            launch_shoot(d, d.stream);
+            CU(launch_shoot(d, d.stream));
             CU(cudaGetLastError());
             CU(cudaEventRecord(d.ev[2], d.stream));
         } else {

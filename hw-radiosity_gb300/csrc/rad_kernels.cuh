@@ -248,6 +248,7 @@ struct State {
     int heavy_on;           // one shooter per step (the fused kernel)
     long long heavy_ns, heavy_ns_split;
     unsigned long long t_start, item_ns;
+    unsigned long long best;  // FP32, one shooter: (ordered key << 32) | slot, the step's maximum
     unsigned items;
     // Groups that took longer than early_ns without being split are stamped
     // (estamp) and listed in early[(s+1)&1]; step s+1 hands them out right
