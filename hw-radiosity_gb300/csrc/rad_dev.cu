@@ -780,28 +780,6 @@ int upload(const Scene<T>& s, const Octree<T>& o, const rad_options& opt, int de
 }
 
 // the shooting kernel of one step; with one shooter per step it also selects the next
-// the shooting kernel of one step; with one shooter per step it also selects the next
-// Launch with programmatic stream serialization: the grid may be scheduled
-// while the previous kernel on the stream is still finishing (k_shoot waits
-// for it with griddepcontrol.wait before reading anything).  In a graph chunk
-// the next step's CTAs then take the SMs its predecessor's tail leaves idle
-// and start the moment it completes.
-template <typename... KArgs, typename... Args>
-cudaError_t launch_overlapped(void (*kernel)(KArgs...), int grid, size_t smem, cudaStream_t s, Args... args) {
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3((unsigned)grid);
-    cfg.blockDim = dim3(kShootThreads);
-    cfg.dynamicSmemBytes = smem;
-    cfg.stream = s;
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-    attr[0].val.programmaticStreamSerializationAllowed = 1;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
-    return cudaLaunchKernelEx(&cfg, kernel, args...);
-}
-
-// the shooting kernel of one step; with one shooter per step it also selects the next
 template <typename T>
 cudaError_t launch_shoot(DevImpl<T>& d, cudaStream_t s) {
     const bool fused = d.P == 1;
