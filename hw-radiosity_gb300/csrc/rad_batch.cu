@@ -129,7 +129,7 @@ k_batch_shoot(const SceneDesc<T>* __restrict__ desc, SceneState* ss, Shooter<T>*
         const SceneDesc<T>& d = desc[s];
         unsigned long long kk = 0;
         int ks = -1;
-        shoot_group<T, COUNT, ONE>(d.S, d.G, sh + d.sh_off, nsh, it.y, lane, d.conv, kk, ks, c);
+        shoot_group<T, COUNT, ONE, true>(d.S, d.G, sh + d.sh_off, nsh, it.y, lane, d.conv, kk, ks, c);
         if (FUSED) {
             warp_max(kk, ks);
             if (lane == 0 && ks >= 0) atomicMax(&ss[s].best, (kk << 32) | (unsigned long long)(unsigned)ks);

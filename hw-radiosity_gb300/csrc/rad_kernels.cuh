@@ -382,17 +382,21 @@ __host__ __device__ __forceinline__ int scan_list(const Grid<T>& G, const T p[3]
 // Brent's cycle detection (one saved state, compared every step, replaced at
 // powers of two) finds any repeated state; the walk then stops, is counted
 // in `loops`, and the ray is treated as blocked (-3).  The state is saved at
-// iterations 0, 2, 6, 14, ... (it + 2 a power of two), Brent's schedule with
-// the power and the count since the last save read off the loop counter.  A
-// walk the reference finishes never repeats a state, so its result is
-// untouched.
-template <typename T, bool COUNT>
+// iterations 0, 2, 6, 14, ... (it + 2 a power of two).  A walk the reference
+// finishes never repeats a state, so its result is untouched.
+// BRENT_IT selects how that schedule is kept, with the same saves and
+// results: read off the loop counter, or held in two counters (the power and
+// the steps since the last save).  Which one compiles faster depends on the kernel the walk is
+// inlined into (measured): the batched kernel takes the loop-counter form
+// (120.8k against 119.4k shots/s on the 256-room batch), the single-scene
+// kernels the counters (the 422k-slot hall: 1,075 against 987 shots/s).
+template <typename T, bool COUNT, bool BRENT_IT = false>
 __host__ __device__ __forceinline__ int walk(const Grid<T>& G, const T p[3], const T v[3], int ban, Cnt& c) {
     T t = 0;
     int prev = -1;
     T q0 = p[0], q1 = p[1], q2 = p[2];
-    T chk_t = (T)-1;                   // Brent: the saved state
-    int chk_prev = -2;
+    T chk_t = (T)-1;                   // Brent: saved state, power, steps since saved
+    int chk_prev = -2, power = 1, lam = 0;
     for (int it = 0; it < G.walk_cap; ++it) {
         if (q0 < G.g0[0] || q0 > G.g1[0] || q1 < G.g0[1] || q1 > G.g1[1] || q2 < G.g0[2] || q2 > G.g1[2])
             return -1;
@@ -400,7 +404,11 @@ __host__ __device__ __forceinline__ int walk(const Grid<T>& G, const T p[3], con
             c.loops++;
             return -3;
         }
-        if (((it + 2) & (it + 1)) == 0) { chk_t = t; chk_prev = prev; }
+        if constexpr (BRENT_IT) {
+            if (((it + 2) & (it + 1)) == 0) { chk_t = t; chk_prev = prev; }
+        } else {
+            if (++lam == power) { chk_t = t; chk_prev = prev; power <<= 1; lam = 0; }
+        }
         if (COUNT) c.cells++;
         const Cell<T> cr = cell_at(G, q0, q1, q2);
         const int leaf = cr.leaf;
@@ -436,9 +444,6 @@ __device__ __forceinline__ int walk_lanes(const Grid<T>& G, const T p[3], const 
     T t = 0;
     int prev = -1;
     T q0 = p[0], q1 = p[1], q2 = p[2];
-    // Brent as in walk, with the power and the count since the last save kept
-    // in registers: the same schedule, but with both walks on the loop-counter
-    // form the kernel that inlines both (form 1) measured 8% slower
     T chk_t = (T)-1;
     int chk_prev = -2, power = 1, lam = 0;
     for (int it = 0; it < G.walk_cap; ++it) {
@@ -540,32 +545,32 @@ __host__ __device__ __forceinline__ bool point_pre(const Shooter<T>& s, const Pa
 }
 
 // CalFF, shade.cpp:107-127: the pre-test is cheap, the walk is not
-template <typename T, bool COUNT, bool WALK>
+template <typename T, bool COUNT, bool WALK, bool BRENT_IT = false>
 __host__ __device__ __forceinline__ T point_ff(const Shooter<T>& s, const Patch<T>& src, const T p[3], const T nd[3], T ndlen,
                                       int logdes, const Grid<T>& G, Cnt& c) {
     T d[3], ff = 0;
     if (!point_pre(s, src, p, nd, ndlen, d, ff)) return 0;
     if (!WALK) return ff;   // pre-test only (reference ray accounting)
     c.rays++;
-    return walk<T, COUNT>(G, p, d, logdes, c) == s.logsrc ? ff : (T)0;
+    return walk<T, COUNT, BRENT_IT>(G, p, d, logdes, c) == s.logsrc ? ff : (T)0;
 }
 
 
 // Shade's per-corner AdaptCalFF(CalFF(...)), shade.cpp:442-450 with the
 // stray ';' at shade.cpp:164: a split source returns ff(half1)+ff(half2); the
 // whole-source result is discarded, so its walk is not cast.
-template <typename T, bool COUNT>
+template <typename T, bool COUNT, bool BRENT_IT = false>
 __host__ __device__ __forceinline__ T corner_ff(const Shooter<T>& s, const T p[3], const T nd[3], T ndlen, int logdes,
                                        const Grid<T>& G, Cnt& c) {
     const unsigned before = c.rays;
     if (!s.split) {
-        const T f = point_ff<T, COUNT, true>(s, s.part[0], p, nd, ndlen, logdes, G, c);
+        const T f = point_ff<T, COUNT, true, BRENT_IT>(s, s.part[0], p, nd, ndlen, logdes, G, c);
         if (COUNT) c.rays_ref += c.rays - before;
         return f;
     }
     if (COUNT && point_ff<T, COUNT, false>(s, s.part[0], p, nd, ndlen, logdes, G, c) > (T)0) c.rays_ref++;
-    const T f1 = point_ff<T, COUNT, true>(s, s.part[1], p, nd, ndlen, logdes, G, c);
-    const T f2 = point_ff<T, COUNT, true>(s, s.part[2], p, nd, ndlen, logdes, G, c);
+    const T f1 = point_ff<T, COUNT, true, BRENT_IT>(s, s.part[1], p, nd, ndlen, logdes, G, c);
+    const T f2 = point_ff<T, COUNT, true, BRENT_IT>(s, s.part[2], p, nd, ndlen, logdes, G, c);
     if (COUNT) c.rays_ref += c.rays - before;
     return f1 + f2;
 }
@@ -629,7 +634,7 @@ __device__ __forceinline__ void flush_counters(State* st, Cnt& c, int lane) {
 // The deposit is the same for every layout: the three corners' form factors
 // meet by shuffle, the group's lane 0 writes its corner's accB, and corner 0's
 // lane 0 keeps the slot's deltaB in the reference's order.
-template <typename T, bool COUNT, int L, bool ONE = false>
+template <typename T, bool COUNT, int L, bool ONE = false, bool BRENT_IT = false>
 __device__ __forceinline__ void shoot_item(const Slots<T>& S, const Grid<T>& G, const Shooter<T>* sh, int nsh, int i0,
                                            int n_item, int lane, T conv, unsigned long long& kk, int& ks, Cnt& c) {
     static_assert(L == 1 || !COUNT, "the counting pass uses the serial walk");
@@ -665,7 +670,7 @@ __device__ __forceinline__ void shoot_item(const Slots<T>& S, const Grid<T>& G, 
             const Q4<T> nn = S.nrm[i];
             const T pv[3] = {pp.x, pp.y, pp.z}, nd[3] = {nn.x, nn.y, nn.z};
             if constexpr (L == 1)
-                ff = corner_ff<T, COUNT>(sh[0], pv, nd, nn.w, parent, G, c);
+                ff = corner_ff<T, COUNT, BRENT_IT>(sh[0], pv, nd, nn.w, parent, G, c);
             else
                 ff = corner_ff_lanes<T, L>(sh[0], pv, nd, nn.w, parent, sub, gmask, G, c);
         }
@@ -722,7 +727,7 @@ __device__ __forceinline__ void shoot_item(const Slots<T>& S, const Grid<T>& G, 
         T ff = 0;
         if (active) {
             if constexpr (L == 1)
-                ff = corner_ff<T, COUNT>(sh[j], pv, nd, ndlen, parent, G, c);
+                ff = corner_ff<T, COUNT, BRENT_IT>(sh[j], pv, nd, ndlen, parent, G, c);
             else
                 ff = corner_ff_lanes<T, L>(sh[j], pv, nd, ndlen, parent, sub, gmask, G, c);
         }
@@ -759,10 +764,10 @@ __device__ __forceinline__ void shoot_item(const Slots<T>& S, const Grid<T>& G, 
 }
 
 // One 10-slot group in the common layout (lanes 3r+v: corner v of slot g*10+r).
-template <typename T, bool COUNT, bool ONE = false>
+template <typename T, bool COUNT, bool ONE = false, bool BRENT_IT = false>
 __device__ __forceinline__ void shoot_group(const Slots<T>& S, const Grid<T>& G, const Shooter<T>* sh, int nsh,
                                             int g, int lane, T conv, unsigned long long& kk, int& ks, Cnt& c) {
-    shoot_item<T, COUNT, 1, ONE>(S, G, sh, nsh, g * kSlotsPerWarp, kSlotsPerWarp, lane, conv, kk, ks, c);
+    shoot_item<T, COUNT, 1, ONE, BRENT_IT>(S, G, sh, nsh, g * kSlotsPerWarp, kSlotsPerWarp, lane, conv, kk, ks, c);
 }
 
 // Shooter record for slot `slot`: normal, |n|, centre, area, unshot energy,
