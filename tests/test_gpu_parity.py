@@ -73,6 +73,40 @@ def test_chunked_runs_equal_one_run(built, workdir):
     assert same_bits(sc.view()["accB"], g["accB"])
 
 
+def test_work_on_the_handle_stream_runs_before_the_next_steps(built, workdir):
+    """rad_dev_stream: a caller's kernel enqueued on the handle's stream (here
+    an L2-sized write, as the bench's flush) runs before the next steps, with
+    no host synchronisation between; the results equal the reference
+    fixture's."""
+    torch = pytest.importorskip("torch")
+    tri, argv, idx = write_case("boxes", workdir)
+    o = capi.options_from_argv(argv)
+    sc = capi.Scene.load(tri, o)
+    tree = capi.Octree(sc, 4)
+    sc.init()
+    sc.prepartition()
+    dv = capi.Device(sc, tree, o)
+    ptr = dv.stream()
+    assert ptr != 0
+    buf = torch.zeros(64 << 20, dtype=torch.float32, device="cuda")
+    ext = torch.cuda.ExternalStream(ptr)
+    total, conv = 0, False
+    for k in range(1, 1 << 20):
+        with torch.cuda.stream(ext):
+            buf.add_(1.0)
+        n, conv, _ = dv.run_timed(1)
+        total += n
+        if conv:
+            break
+    torch.cuda.synchronize()
+    assert float(buf[0]) == float(k) and float(buf[-1]) == float(k)
+    dv.download(sc)
+    g = golden("boxes")
+    assert conv and total == idx["steps"]
+    assert np.array_equal(dv.trace(), g["trace"])
+    assert same_bits(sc.view()["accB"], g["accB"])
+
+
 @pytest.mark.parametrize("P", [2, 5])
 def test_parallel_shooters_equal_oracle(built, workdir, P):
     s = scenes.room_with_boxes(8, 4, 1, seed=21, size=20.0)
