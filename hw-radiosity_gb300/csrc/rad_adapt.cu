@@ -576,12 +576,13 @@ int spec_enqueue(AdaptImpl<T>& a, const Slots<T>& S, int n0, long long start, lo
     return RAD_OK;
 }
 
-// Whether point t of the current speculation is on the host.  The host never
-// waits for one: a walk on the GPU takes longer than the same walk on the
-// host, so a point the device has not written yet is evaluated on the host
-// (the same arithmetic, the same value) while the kernel runs ahead to the
-// receivers after it.  A failed kernel is reported by the next step's stream
-// synchronisation.
+// Whether point t of the current speculation is on the host.  Racing, the
+// host never waits for one: a walk on the GPU takes longer than the same walk
+// on the host, so a point the device has not written yet is evaluated on the
+// host (the same arithmetic, the same value) while the kernel runs ahead to
+// the receivers after it.  Waiting, device_points has already waited for the
+// whole speculation, so every point it wrote is there.  A failed kernel is
+// reported by the next step's stream synchronisation.
 template <typename T>
 bool spec_ready(const AdaptImpl<T>& a, long long t) {
     return __atomic_load_n(a.h_stag + t, __ATOMIC_ACQUIRE) == a.sp_gen;
