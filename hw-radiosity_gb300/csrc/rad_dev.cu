@@ -114,8 +114,23 @@ k_shoot(Slots<T> S, Grid<T> G, Shooter<T>* shooters, State* st, Partial* __restr
     constexpr int kHeavySlots = heavy_slots<HL>(), kHeavyItems = heavy_items<HL>();
     const int n_heavy_items = split ? st->heavy_n[s & 1] * kHeavyItems : 0;
     const int n_early = split ? st->early_n[s & 1] : 0;
-    // each warp's first item is its own index; later ones come from the queue
+    // The last groups of the slot order go out as split items (4 lanes per
+    // corner, kHeavySlots slots each), like the heavy ones: handed out when
+    // the queue is nearly empty, a whole group would start long walks that
+    // the rest of the grid, idle by then, waits for; split, its walks spread
+    // over the idle warps.  One group per 16 resident warps, at most a
+    // twentieth of the groups; only where split items use several lanes and
+    // a step is about one wave of groups (at most two per resident warp: on
+    // the 61k-slot room the step fell from 95.5 to 94.7 us flushed and from
+    // 87.6 to 84.4 us in graph chunks).  With many groups per warp the slow
+    // groups' own split (the heavy part) serves better: the 422k-slot hall
+    // in form 1 fell from 812 to 663 shots/s with a tail.  (Form 1 on the hall
+    // measures 690 against 810 shots/s even without one, from the registers
+    // this code takes; the hall runs form 2, unchanged at 1,066.)
     const int n_warps = (int)gridDim.x * (kShootThreads / 32);
+    const int n_tail = (split && HL > 1 && n_groups <= 2 * n_warps) ? imin(n_groups / 20, n_warps / 16) : 0;
+    const int n_whole = n_groups - n_tail;
+    // each warp's first item is its own index; later ones come from the queue
     int first = (int)blockIdx.x * (kShootThreads / 32) + wid;
     for (;;) {
         int g = first;
@@ -126,6 +141,7 @@ k_shoot(Slots<T> S, Grid<T> G, Shooter<T>* shooters, State* st, Partial* __restr
         first = -1;
         int grp, i0, n_item;
         const unsigned long long t_item = global_ns();
+        bool tail = false;
         if (g < n_heavy_items) {
             grp = st->heavy[(s & 1) * n_groups + g / kHeavyItems];
             const int part = (g % kHeavyItems) * kHeavySlots;
@@ -133,16 +149,28 @@ k_shoot(Slots<T> S, Grid<T> G, Shooter<T>* shooters, State* st, Partial* __restr
             n_item = imin(kHeavySlots, kSlotsPerWarp - part);
         } else {
             const int j = g - n_heavy_items;
+            int q = 0;
             if (j < n_early) {
                 grp = st->early[(s & 1) * n_groups + j];
-            } else {
+            } else if (j - n_early < n_whole) {
                 grp = j - n_early;
-                if (grp >= n_groups) break;
                 if (split && __ldcg(&st->estamp[grp]) >= s) continue;   // it was in the early part
+            } else {                                                     // the tail's split items
+                q = j - n_early - n_whole;
+                if (q >= n_tail * kHeavyItems) break;
+                grp = n_whole + q / kHeavyItems;
+                tail = true;
+                if (__ldcg(&st->estamp[grp]) >= s) continue;
             }
             if (split && __ldcg(&st->stamp[grp]) >= s) continue;   // its items are in the heavy part
-            i0 = grp * kSlotsPerWarp;
-            n_item = kSlotsPerWarp;
+            if (tail) {
+                const int part = (q % kHeavyItems) * kHeavySlots;
+                i0 = grp * kSlotsPerWarp + part;
+                n_item = imin(kHeavySlots, kSlotsPerWarp - part);
+            } else {
+                i0 = grp * kSlotsPerWarp;
+                n_item = kSlotsPerWarp;
+            }
         }
         // one call site when every item is cast one lane per corner: the
         // walk is inlined once, which keeps the register count down
@@ -156,23 +184,26 @@ k_shoot(Slots<T> S, Grid<T> G, Shooter<T>* shooters, State* st, Partial* __restr
         if constexpr (HL == 1 || COUNT) {
             shoot_item<T, COUNT, 1, FUSED>(S, Gs, sh, nsh, i0, n_item, lane, conv, kk, ks, c);
         } else {
-            if (g < n_heavy_items)
+            if (g < n_heavy_items || tail)
                 shoot_item<T, false, HL, kOneHeavy>(S, Gs, sh, nsh, i0, n_item, lane, conv, kk, ks, c);
             else
                 shoot_item<T, COUNT, 1, FUSED>(S, Gs, sh, nsh, i0, n_item, lane, conv, kk, ks, c);
         }
         if (split && lane == 0) {
             const long long dt = (long long)(global_ns() - t_item);
-            if (g >= n_heavy_items) {
+            if (g >= n_heavy_items && !tail) {
                 atomicAdd(&st->item_ns, (unsigned long long)dt);
                 atomicAdd(&st->items, 1u);
             }
-            if (dt > (g < n_heavy_items ? st->heavy_ns_split : st->heavy_ns)) {
+            // a tail group is not marked: its later items read its stamp to
+            // tell whether the heavy part already shot it, and the tail
+            // splits it again in the next step
+            if (!tail && dt > (g < n_heavy_items ? st->heavy_ns_split : st->heavy_ns)) {
                 if (atomicMax(&st->stamp[grp], s + 1) < s + 1) {
                     const int q = atomicAdd(&st->heavy_n[(s + 1) & 1], 1);
                     st->heavy[((s + 1) & 1) * n_groups + q] = grp;
                 }
-            } else if (g >= n_heavy_items && dt > st->early_ns) {
+            } else if (!tail && g >= n_heavy_items && dt > st->early_ns) {
                 st->estamp[grp] = s + 1;
                 const int q = atomicAdd(&st->early_n[(s + 1) & 1], 1);
                 st->early[((s + 1) & 1) * n_groups + q] = grp;
