@@ -1,9 +1,17 @@
-// Scratch of the scene-preparation kernels (octree overlap tests, neighbour
-// links): per host thread and device, a stream and grow-only device buffers
-// kept between calls.  A batch of small scenes then pays neither a stream
-// creation nor a synchronising cudaFree per scene.  Each call finishes its
-// work on the stream before it returns, so consecutive calls on one thread
-// can share the buffers; calls from different threads use their own.
+// Host-side resources of scene preparation and handle creation:
+//   PrepWorkspace  per host thread and device, a stream and grow-only device
+//                  buffers for the preparation kernels (octree overlap tests,
+//                  neighbour links, table expansion), kept between calls;
+//   PinnedStage    per host thread, grow-only pinned staging for uploads and
+//                  downloads;
+//   HostPool       the process's pool of host threads for the packing passes
+//                  (split_range, for_each_item, copy_segments);
+//   HostLayout, DevBlock  offsets of pieces in one staging buffer or one
+//                  device allocation.
+// A batch of small scenes then pays neither a stream creation nor a
+// synchronising cudaFree per scene.  Each call finishes its work on the
+// stream before it returns, so consecutive calls on one thread can share the
+// buffers; calls from different threads use their own.
 #pragma once
 #include <cuda_runtime.h>
 
